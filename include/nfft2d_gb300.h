@@ -1,0 +1,186 @@
+/*
+ * nfft2d_gb300.h -- C ABI of the GB300 (sm_103a) 2D NFFT.
+ *
+ * One shared library, libnfft2d_gb300.so, exports every function declared
+ * here with C linkage: plain pointers, sizes and status codes, no C++ or
+ * torch types.  Array arguments are DEVICE pointers owned by the caller
+ * (as in the reference, NFFT/NFFT2_2D.cuh:8-11 and NFFT/NDFT2_2D.cuh:4-6);
+ * work buffers are owned by a plan, allocated once at plan creation /
+ * set_points, never per call.
+ *
+ * Conventions (shared with the reference, NFFT/NFFT2_2D.cu:23,66,124-125 and
+ * BP_FBP_FFBP/NFFT1_2D.m:17-18,29-30,55):
+ *   - a coefficient array F is N1 x N2 complex, row-major, element
+ *     F[i*N2 + j] holds frequency (k1, k2) = (i - N1/2, j - N2/2);
+ *   - point p has coordinates (x1_p, x2_p); x1 pairs with N1 (rows);
+ *   - in GRID units a coordinate spans one period over [-N/2, N/2) (the
+ *     reference's units); in UNIT units over [-0.5, 0.5); in RADIANS over
+ *     [-pi, pi).  Any real value is accepted and wrapped periodically;
+ *   - complex values are interleaved (re, im): float2 for NFFT2D_F32 plans,
+ *     double2 for NFFT2D_F64 plans.
+ *
+ * Transforms (x in grid units):
+ *   type 2 ("forward", reference NFFT1_2D, non-equispaced results):
+ *       f_p = sum_k F_k exp(sign * 2 pi i (k1 x1_p / N1 + k2 x2_p / N2))
+ *   type 1 (spreading, reference NFFT2_2D, non-equispaced data):
+ *       F_k = sum_p f_p exp(sign * 2 pi i (k1 x1_p / N1 + k2 x2_p / N2))
+ * The reference uses sign = -1 for both (NFFT2_2D.m:63, NFFT1_2D.m:55), so
+ * its NFFT2_2D is the transpose of NFFT1_2D; the Hermitian adjoint of the
+ * forward is type 1 with sign = +1.
+ *
+ * Every function returns an int status (NFFT2D_OK = 0, negative on error)
+ * and never exits the process.  Transforms are asynchronous on the plan's
+ * stream; device-side faults that a kernel detects itself (a bounded wait
+ * that ran out, a corrupted bin record) are latched in the plan and
+ * reported by nfft2d_synchronize().
+ */
+#ifndef NFFT2D_GB300_H
+#define NFFT2D_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define NFFT2D_OK                   0
+#define NFFT2D_ERR_INVALID_ARG     -1  /* bad size, null pointer, bad enum       */
+#define NFFT2D_ERR_OOM             -2  /* device or host allocation failed        */
+#define NFFT2D_ERR_CUDA            -3  /* a CUDA runtime call failed              */
+#define NFFT2D_ERR_CUFFT           -4  /* a cuFFT call failed                     */
+#define NFFT2D_ERR_NO_POINTS       -5  /* transform called before set_points      */
+#define NFFT2D_ERR_NONFINITE       -6  /* a coordinate was NaN or +-Inf           */
+#define NFFT2D_ERR_DEVICE_TIMEOUT  -7  /* a bounded device-side wait ran out      */
+#define NFFT2D_ERR_DEVICE_BOUNDS   -8  /* a kernel rejected an out-of-tile record */
+#define NFFT2D_ERR_UNSUPPORTED     -9  /* valid request this build does not serve */
+#define NFFT2D_ERR_INTERNAL       -10
+
+/* ---- enums ------------------------------------------------------------ */
+#define NFFT2D_F32 0   /* complex64 data, FP32 kernels (FP64 plan-time math) */
+#define NFFT2D_F64 1   /* complex128 data, FP64 kernels                      */
+
+#define NFFT2D_COORD_F32 0
+#define NFFT2D_COORD_F64 1
+
+#define NFFT2D_UNITS_GRID    0  /* reference units: period N_d             */
+#define NFFT2D_UNITS_UNIT    1  /* period 1, [-0.5, 0.5)                   */
+#define NFFT2D_UNITS_RADIANS 2  /* period 2*pi, [-pi, pi)                  */
+
+/* Kernel variants for the gather (type 2) and the spread (type 1). */
+#define NFFT2D_VARIANT_AUTO   0
+#define NFFT2D_VARIANT_TILED  1  /* binned tiles staged by TMA in shared memory */
+#define NFFT2D_VARIANT_DIRECT 2  /* sorted points, taps read straight from L2   */
+
+typedef struct nfft2d_plan_s *nfft2d_plan;
+
+typedef struct {
+    int N1, N2;            /* coefficient grid                                  */
+    double sigma;          /* oversampling factor (reference c)                 */
+    int K;                 /* window half-width: 2K+1 taps per dimension        */
+    int precision;         /* NFFT2D_F32 / NFFT2D_F64                           */
+    int n1, n2;            /* oversampled grid sigma*N1 x sigma*N2              */
+    int halo;              /* periodic halo cells around the oversampled grid   */
+    int rows, cols;        /* padded grid allocation: whole tiles + halo each side */
+    int tile;              /* bin tile edge, in oversampled cells               */
+    int tiles1, tiles2;    /* number of tiles per dimension                     */
+    int patch_rows, patch_cols; /* shared-memory patch of one tile with halo    */
+    int chunk;             /* maximum points per work item                      */
+    int gather_variant, spread_variant;
+    long long M;           /* points currently set (0 before set_points)        */
+    long long n_chunks;    /* work items built by the last set_points           */
+    size_t workspace_bytes;/* device bytes owned by the plan                    */
+} nfft2d_info;
+
+typedef struct {
+    int tile;              /* 0 = default; else 8, 16, 32 or 64                 */
+    int chunk;             /* 0 = default; else points per work item (>= 32)    */
+    int gather_variant;    /* NFFT2D_VARIANT_*                                  */
+    int spread_variant;    /* NFFT2D_VARIANT_*                                  */
+    int compensated;       /* -1 = default (on); 0 off; 1 on (FP32 gather)      */
+} nfft2d_tuning;
+
+/* Stage times in milliseconds, from CUDA events recorded on the plan's
+ * stream while timing is enabled.  Each field holds the most recent run of
+ * that stage: a type-2 call refreshes pad / fft_type2 / halo_fill / gather,
+ * a type-1 call refreshes spread / fold / fft_type1 / crop, set_points
+ * refreshes sort; fields of stages that never ran are 0. */
+typedef struct {
+    float sort_ms;         /* set_points: binning + counting sort               */
+    float pad_ms;          /* type 2: deapodize + zero-pad                      */
+    float fft_type2_ms;    /* type 2: cuFFT on the oversampled grid             */
+    float halo_fill_ms;    /* type 2: periodic halo fill                        */
+    float gather_ms;       /* type 2: windowed gather (or coordinate gradient)  */
+    float spread_ms;       /* type 1: zero the grid + windowed spread           */
+    float fold_ms;         /* type 1: fold the halo onto the interior           */
+    float fft_type1_ms;    /* type 1: cuFFT on the oversampled grid             */
+    float crop_ms;         /* type 1: crop + deapodize                          */
+} nfft2d_timings;
+
+/* ---- plan life cycle --------------------------------------------------
+ * Replaces the reference's process-global cuFFT plan
+ * (NFFT/NFFT2_2D.cu:11,49-55: Calculate_cuFFT_plan_C2C_NFFT2_2D,
+ * Calculate_cuFFT_plan_Z2Z_NFFT2_2D, Destroy_cuFFT_plan_NFFT2_2D) and the
+ * per-call cudaMalloc/Kernel_Bessel work of NFFT2_2D_GPU (:333-367).
+ * sigma*N1 and sigma*N2 must be even integers >= N and >= 2K+2; N1, N2 even;
+ * 2 <= K <= 8; sigma >= 1.25.  stream may be NULL (legacy default stream). */
+int nfft2d_plan_create(nfft2d_plan *plan, int N1, int N2, double sigma, int K, int precision, void *stream);
+int nfft2d_plan_destroy(nfft2d_plan plan);
+int nfft2d_set_stream(nfft2d_plan plan, void *stream);
+int nfft2d_set_tuning(nfft2d_plan plan, const nfft2d_tuning *tuning);
+int nfft2d_get_info(nfft2d_plan plan, nfft2d_info *info);
+
+/* Host-only: the layout a plan with these parameters would use (no GPU
+ * needed).  tile = 0 picks the default. */
+int nfft2d_layout_query(int N1, int N2, double sigma, int K, int precision, int tile, nfft2d_info *info);
+
+/* ---- points -------------------------------------------------------------
+ * Bins and sorts the M points into tiles of the oversampled grid (the
+ * reference recomputes mu = rint(c*x) per call inside
+ * Interpolation_NFFT2_2D_GPUKernel, NFFT2_2D.cu:163-173).  The coordinate
+ * reduction runs in FP64.  Synchronizes the plan's stream.  M = 0 is valid
+ * (transforms then produce zeros). */
+int nfft2d_set_points(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype, int units);
+
+/* ---- transforms ---------------------------------------------------------
+ * nfft2d_forward   : type 2, sign -1  (BP_FBP_FFBP/NFFT1_2D.m:1-69)
+ * nfft2d_adjoint   : type 1, sign +1  (Hermitian adjoint of nfft2d_forward)
+ * nfft2d_spread_ref: type 1, sign -1  (NFFT/NFFT2_2D.cu:329-495 and
+ *                    NFFT/NFFT2/Matlab/NFFT2_2D.m:1-72)
+ * f has M entries in the caller's point order; F has N1*N2 entries. */
+int nfft2d_forward(nfft2d_plan plan, const void *F, void *f);
+int nfft2d_adjoint(nfft2d_plan plan, const void *f, void *F);
+int nfft2d_spread_ref(nfft2d_plan plan, const void *f, void *F);
+int nfft2d_type2(nfft2d_plan plan, int sign, const void *F, void *f);
+int nfft2d_type1(nfft2d_plan plan, int sign, const void *f, void *F);
+
+/* Gradient of a type-2 transform w.r.t. the point coordinates, contracted
+ * with a cotangent v (M complex):
+ *     g1[p] = Re( conj(v_p) * d f_p / d x1_p ),  g2 likewise for x2,
+ * in the units given to set_points; g1, g2 are M reals of the plan's
+ * precision.  For L = ||f - y||^2 pass v = 2 (f - y).  No reference
+ * counterpart (added differentiation of the forward gather). */
+int nfft2d_grad_x(nfft2d_plan plan, int sign, const void *F, const void *v, void *g1, void *g2);
+
+/* ---- status / timing ---------------------------------------------------- */
+int nfft2d_synchronize(nfft2d_plan plan);
+int nfft2d_enable_timing(nfft2d_plan plan, int on);
+int nfft2d_get_timings(nfft2d_plan plan, nfft2d_timings *t);
+const char *nfft2d_status_string(int status);
+int nfft2d_device_count(void);
+
+/* ---- exact direct sum ----------------------------------------------------
+ * Matrix-free FP64 replacement of NDFT2_2D_GPU (NFFT/NDFT2_2D.cu:37-72):
+ *     out[q] = sum_p in[p] exp(sign * 2 pi i (u_q X_p / Nu + v_q Y_p / Nv))
+ * for M points and N frequencies (u_q, v_q arbitrary reals); in/out are
+ * double2.  The reference uses sign = -1, builds an explicit M x N matrix
+ * and dumps it to a file; this builds no matrix and writes no file. */
+int nfft2d_ndft2d_f64(const double *X, const double *Y, const double *u, const double *v,
+                      const void *in, void *out, int Nu, int Nv, long long M, long long N,
+                      int sign, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NFFT2D_GB300_H */

@@ -1,0 +1,135 @@
+"""ctypes binding of libnfft2d_gb300.so (the C ABI declared in
+include/nfft2d_gb300.h).
+
+The library is built in-tree (``miscellaneous_gb300/lib``) by
+``miscellaneous_gb300.build.build()``.  Loading fails loudly when it is
+missing: there is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libnfft2d_gb300.so")
+HEADER_PATH = os.path.join(os.path.dirname(_PKG), "include", "nfft2d_gb300.h")
+
+# status codes (nfft2d_gb300.h)
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_OOM = -2
+ERR_CUDA = -3
+ERR_CUFFT = -4
+ERR_NO_POINTS = -5
+ERR_NONFINITE = -6
+ERR_DEVICE_TIMEOUT = -7
+ERR_DEVICE_BOUNDS = -8
+ERR_UNSUPPORTED = -9
+ERR_INTERNAL = -10
+
+F32 = 0
+F64 = 1
+COORD_F32 = 0
+COORD_F64 = 1
+UNITS = {"grid": 0, "unit": 1, "radians": 2}
+VARIANT_AUTO, VARIANT_TILED, VARIANT_DIRECT = 0, 1, 2
+
+
+class Info(ctypes.Structure):
+    _fields_ = [
+        ("N1", ctypes.c_int), ("N2", ctypes.c_int), ("sigma", ctypes.c_double), ("K", ctypes.c_int),
+        ("precision", ctypes.c_int), ("n1", ctypes.c_int), ("n2", ctypes.c_int), ("halo", ctypes.c_int),
+        ("rows", ctypes.c_int), ("cols", ctypes.c_int), ("tile", ctypes.c_int), ("tiles1", ctypes.c_int),
+        ("tiles2", ctypes.c_int), ("patch_rows", ctypes.c_int), ("patch_cols", ctypes.c_int),
+        ("chunk", ctypes.c_int), ("gather_variant", ctypes.c_int), ("spread_variant", ctypes.c_int),
+        ("M", ctypes.c_longlong), ("n_chunks", ctypes.c_longlong), ("workspace_bytes", ctypes.c_size_t),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_int), ("chunk", ctypes.c_int), ("gather_variant", ctypes.c_int),
+                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int)]
+
+
+class Timings(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in
+                ("sort_ms", "pad_ms", "fft_type2_ms", "halo_fill_ms", "gather_ms", "spread_ms", "fold_ms",
+                 "fft_type1_ms", "crop_ms")]
+
+    def as_dict(self) -> dict:
+        return {name: float(getattr(self, name)) for name, _ in self._fields_}
+
+
+class NFFT2DError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = status_string(status) if _lib is not None else str(status)
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_LL = ctypes.c_longlong
+_D = ctypes.c_double
+
+_SIGNATURES = {
+    "nfft2d_plan_create": (_I, [ctypes.POINTER(_P), _I, _I, _D, _I, _I, _P]),
+    "nfft2d_plan_destroy": (_I, [_P]),
+    "nfft2d_set_stream": (_I, [_P, _P]),
+    "nfft2d_set_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
+    "nfft2d_get_info": (_I, [_P, ctypes.POINTER(Info)]),
+    "nfft2d_layout_query": (_I, [_I, _I, _D, _I, _I, _I, ctypes.POINTER(Info)]),
+    "nfft2d_set_points": (_I, [_P, _LL, _P, _P, _I, _I]),
+    "nfft2d_forward": (_I, [_P, _P, _P]),
+    "nfft2d_adjoint": (_I, [_P, _P, _P]),
+    "nfft2d_spread_ref": (_I, [_P, _P, _P]),
+    "nfft2d_type2": (_I, [_P, _I, _P, _P]),
+    "nfft2d_type1": (_I, [_P, _I, _P, _P]),
+    "nfft2d_grad_x": (_I, [_P, _I, _P, _P, _P, _P]),
+    "nfft2d_synchronize": (_I, [_P]),
+    "nfft2d_enable_timing": (_I, [_P, _I]),
+    "nfft2d_get_timings": (_I, [_P, ctypes.POINTER(Timings)]),
+    "nfft2d_status_string": (ctypes.c_char_p, [_I]),
+    "nfft2d_device_count": (_I, []),
+    "nfft2d_ndft2d_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _LL, _LL, _I, _P]),
+}
+
+
+def header_functions(path: str = HEADER_PATH) -> list[str]:
+    """Names of every function declared in include/nfft2d_gb300.h."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nfft2d_[a-z0-9_]+)\s*\(", text)))
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: the CUDA extension has not been built "
+            "(run `python -c 'import __graft_entry__ as g; g.build()'`). "
+            "This package has no CPU fallback.")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    return load().nfft2d_status_string(int(status)).decode()
+
+
+def check(status: int, what: str = "") -> None:
+    if status != OK:
+        raise NFFT2DError(status, what)

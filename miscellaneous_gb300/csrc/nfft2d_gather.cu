@@ -1,0 +1,326 @@
+// nfft2d_gather.cu -- type-2 windowed gather at the nonuniform points (the
+// hot loop of BP_FBP_FFBP/NFFT1_2D.m:61-67) and its derivative w.r.t. the
+// point coordinates.
+//
+// TILED variant (FP32 plans): points are binned into T x T tiles of the
+// oversampled grid and sorted row-major by cell inside each tile.  A
+// persistent CTA walks work items (tile, point range); for each it stages the
+// tile's (T+2K) x (T+2Ke) patch of the padded grid into shared memory with
+// one TMA load (cp.async.bulk.tensor.2d, completion on an mbarrier),
+// double-buffered so the next patch streams in while the current one is
+// consumed.  Each thread evaluates the 2(2K+1) separable window weights of
+// its point once and sums the (2K+1)^2 taps from shared memory; adjacent
+// lanes hold adjacent cells, so a warp's reads of one tap hit consecutive
+// addresses.  Row partial sums use FMA; the sum over rows is compensated
+// (TwoSum) when enabled.
+//
+// DIRECT variant (both precisions): one thread per sorted point reads its
+// taps straight from the padded grid (L1/L2), no shared memory.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "nfft2d_device.cuh"
+#include "nfft2d_internal.h"
+#include "nfft2d_kargs.cuh"
+
+namespace nfft2d {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int K>
+__device__ __forceinline__ void issue_patch(const CUtensorMap *map, const int4 *__restrict__ chunks, int c,
+                                            float2 *dst, uint64_t *bar, const Geom &g) {
+    const int tile = __ldg(&chunks[c].x);
+    const int tr = tile / g.tiles2, tc = tile - tr * g.tiles2;
+    const int x = 2 * (g.H + tc * g.T - g.Ke);  // FP32 element index, multiple of 4 (16 bytes)
+    const int y = g.H + tr * g.T - K;
+    mbar_arrive_expect_tx(bar, static_cast<uint32_t>(g.PR * g.PC * sizeof(float2)));
+    tma_load_2d(dst, map, bar, x, y);
+}
+
+// MODE 0: f = gather(grid);  MODE 1: coordinate gradient contracted with vin.
+template <int K, bool COMP, int MODE>
+__global__ void __launch_bounds__(kThreads) k_gather_tiled(const __grid_constant__ CUtensorMap tmap,
+                                                           const Rec32 *__restrict__ recs,
+                                                           const int4 *__restrict__ chunks, float2 *__restrict__ out,
+                                                           const float2 *__restrict__ vin, float *__restrict__ g1,
+                                                           float *__restrict__ g2, const KArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_ok;
+    constexpr int W = 2 * K + 1;
+    const Geom g = a.g;
+    const int pstride = patch_stride_elems(g);
+    // TMA shared-memory operands: 128-byte aligned (the launch adds 128 bytes of slack)
+    float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    const int n = a.n_chunks;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) < n) issue_patch<K>(&tmap, chunks, blockIdx.x, bufs, &bars[0], g);
+
+    uint32_t phase = 0;  // bit b: parity to wait for on bars[b]
+    int it = 0;
+    for (int c = blockIdx.x; c < n; c += gridDim.x, ++it) {
+        const int b = it & 1;
+        const uint32_t par = (phase >> b) & 1u;
+        const int cnext = c + gridDim.x;
+        if (threadIdx.x == 0) {
+            if (cnext < n) {
+                fence_proxy_async_smem();
+                issue_patch<K>(&tmap, chunks, cnext, bufs + (b ^ 1) * pstride, &bars[b ^ 1], g);
+            }
+            s_ok = mbar_wait_bounded(&bars[b], par) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_ok) {
+            if (threadIdx.x == 0) {
+                latch_error(a.status, kErrTimeout);
+                if (cnext < n) (void)mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+            }
+            return;
+        }
+        if (threadIdx.x != 0) (void)mbar_wait_bounded(&bars[b], par);  // completed: acquire only
+        phase ^= (1u << b);
+
+        const int4 ch = __ldg(&chunks[c]);
+        const int tr = ch.x / g.tiles2, tc = ch.x - tr * g.tiles2;
+        const int r0 = tr * g.T, c0 = tc * g.T;
+        const float2 *patch = bufs + b * pstride;
+        for (int i = threadIdx.x; i < ch.z; i += kThreads) {
+            const int4 raw = __ldg(reinterpret_cast<const int4 *>(recs) + ch.y + i);
+            const float t1 = __int_as_float(raw.x), t2 = __int_as_float(raw.y);
+            const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
+            const int lr = mu1 - r0, lc = mu2 - c0;
+            if (static_cast<unsigned>(lr) >= static_cast<unsigned>(g.T) ||
+                static_cast<unsigned>(lc) >= static_cast<unsigned>(g.T)) {
+                latch_error(a.status, kErrBounds);
+                continue;
+            }
+            float w1[W], w2[W];
+            weights_f32<K>(t1, w1, a.alpha, a.cn, a.kp);
+            weights_f32<K>(t2, w2, a.alpha, a.cn, a.kp);
+            const float2 *base = patch + lr * g.PC + lc + (g.Ke - K);
+            if (MODE == 0) {
+                float sx = 0.f, sy = 0.f, ex = 0.f, ey = 0.f;
+#pragma unroll
+                for (int r = 0; r < W; ++r) {
+                    const float2 *row = base + r * g.PC;
+                    float rx = 0.f, ry = 0.f;
+#pragma unroll
+                    for (int q = 0; q < W; ++q) {
+                        const float2 v = row[q];
+                        rx = fmaf(w2[q], v.x, rx);
+                        ry = fmaf(w2[q], v.y, ry);
+                    }
+                    if (COMP) {
+                        float e;
+                        two_sum(sx, __fmul_rn(w1[r], rx), sx, e);
+                        ex = __fadd_rn(ex, e);
+                        two_sum(sy, __fmul_rn(w1[r], ry), sy, e);
+                        ey = __fadd_rn(ey, e);
+                    } else {
+                        sx = fmaf(w1[r], rx, sx);
+                        sy = fmaf(w1[r], ry, sy);
+                    }
+                }
+                out[raw.w] = make_float2(sx + ex, sy + ey);
+            } else {
+                float d1[W], d2[W];
+                dweights_f32<K>(t1, w1, d1, a.alpha, a.cn);
+                dweights_f32<K>(t2, w2, d2, a.alpha, a.cn);
+                float ax = 0.f, ay = 0.f, bx = 0.f, by = 0.f;
+#pragma unroll
+                for (int r = 0; r < W; ++r) {
+                    const float2 *row = base + r * g.PC;
+                    float rx = 0.f, ry = 0.f, qx = 0.f, qy = 0.f;
+#pragma unroll
+                    for (int q = 0; q < W; ++q) {
+                        const float2 v = row[q];
+                        rx = fmaf(w2[q], v.x, rx);
+                        ry = fmaf(w2[q], v.y, ry);
+                        qx = fmaf(d2[q], v.x, qx);
+                        qy = fmaf(d2[q], v.y, qy);
+                    }
+                    ax = fmaf(d1[r], rx, ax);
+                    ay = fmaf(d1[r], ry, ay);
+                    bx = fmaf(w1[r], qx, bx);
+                    by = fmaf(w1[r], qy, by);
+                }
+                const float2 v = __ldg(&vin[raw.w]);
+                g1[raw.w] = a.ds1 * (v.x * ax + v.y * ay);
+                g2[raw.w] = a.ds2 * (v.x * bx + v.y * by);
+            }
+        }
+        __syncthreads();  // buffer b is free for the prefetch issued next iteration
+    }
+}
+
+template <typename Real>
+struct CxOf;
+template <>
+struct CxOf<float> {
+    using type = float2;
+};
+template <>
+struct CxOf<double> {
+    using type = double2;
+};
+
+template <int K, typename Real>
+__device__ __forceinline__ void weights_any(Real t, Real (&w)[2 * K + 1], const KArgs &a) {
+    if constexpr (sizeof(Real) == 4)
+        weights_f32<K>(t, w, a.alpha, a.cn, a.kp);
+    else
+        weights_f64<K>(t, w, a.alpha_d, a.cn_d);
+}
+
+template <int K, typename Real>
+__device__ __forceinline__ void dweights_any(Real t, const Real (&w)[2 * K + 1], Real (&dw)[2 * K + 1],
+                                             const KArgs &a) {
+    if constexpr (sizeof(Real) == 4)
+        dweights_f32<K>(t, w, dw, a.alpha, a.cn);
+    else
+        dweights_f64<K>(t, dw, a.alpha_d, a.cn_d);
+}
+
+template <int K, typename Real, typename RecT, int MODE>
+__global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<Real>::type *__restrict__ grid,
+                                                            const RecT *__restrict__ recs,
+                                                            typename CxOf<Real>::type *__restrict__ out,
+                                                            const typename CxOf<Real>::type *__restrict__ vin,
+                                                            Real *__restrict__ g1, Real *__restrict__ g2,
+                                                            const KArgs a) {
+    using Cx = typename CxOf<Real>::type;
+    constexpr int W = 2 * K + 1;
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.M) return;
+    const RecT r = recs[i];
+    const int mu1 = static_cast<int>(static_cast<unsigned>(r.mu) >> 16), mu2 = r.mu & 0xFFFF;
+    const Geom g = a.g;
+    if (mu1 >= g.n1 || mu2 >= g.n2) {
+        latch_error(a.status, kErrBounds);
+        return;
+    }
+    const Cx *base = grid + static_cast<size_t>(mu1 + g.H - K) * g.C + (mu2 + g.H - K);
+    Real w1[W], w2[W];
+    weights_any<K, Real>(static_cast<Real>(r.t1), w1, a);
+    weights_any<K, Real>(static_cast<Real>(r.t2), w2, a);
+    if (MODE == 0) {
+        Real sx = 0, sy = 0;
+#pragma unroll
+        for (int rr = 0; rr < W; ++rr) {
+            const Cx *row = base + static_cast<size_t>(rr) * g.C;
+            Real rx = 0, ry = 0;
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                const Cx v = __ldg(row + q);
+                rx += w2[q] * v.x;
+                ry += w2[q] * v.y;
+            }
+            sx += w1[rr] * rx;
+            sy += w1[rr] * ry;
+        }
+        Cx o;
+        o.x = sx;
+        o.y = sy;
+        out[r.orig] = o;
+    } else {
+        Real d1[W], d2[W];
+        dweights_any<K, Real>(static_cast<Real>(r.t1), w1, d1, a);
+        dweights_any<K, Real>(static_cast<Real>(r.t2), w2, d2, a);
+        Real ax = 0, ay = 0, bx = 0, by = 0;
+#pragma unroll
+        for (int rr = 0; rr < W; ++rr) {
+            const Cx *row = base + static_cast<size_t>(rr) * g.C;
+            Real rx = 0, ry = 0, qx = 0, qy = 0;
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                const Cx v = __ldg(row + q);
+                rx += w2[q] * v.x;
+                ry += w2[q] * v.y;
+                qx += d2[q] * v.x;
+                qy += d2[q] * v.y;
+            }
+            ax += d1[rr] * rx;
+            ay += d1[rr] * ry;
+            bx += w1[rr] * qx;
+            by += w1[rr] * qy;
+        }
+        const Cx v = __ldg(&vin[r.orig]);
+        if constexpr (sizeof(Real) == 4) {
+            g1[r.orig] = a.ds1 * (v.x * ax + v.y * ay);
+            g2[r.orig] = a.ds2 * (v.x * bx + v.y * by);
+        } else {
+            g1[r.orig] = a.ds1_d * (v.x * ax + v.y * ay);
+            g2[r.orig] = a.ds2_d * (v.x * bx + v.y * by);
+        }
+    }
+}
+
+template <typename KernelT>
+cudaError_t prepare_smem(KernelT kernel, int smem) {
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return cudaSuccess;
+}
+
+template <int K, int MODE>
+cudaError_t launch_K(const nfft2d_plan_s *p, void *f, const void *v, void *g1, void *g2) {
+    const KArgs a = make_kargs(p);
+    if (p->precision == NFFT2D_F32 && p->gather_variant == NFFT2D_VARIANT_TILED) {
+        if (p->n_chunks == 0) return cudaSuccess;
+        const int smem = 2 * patch_stride_elems(p->g) * static_cast<int>(sizeof(float2)) + 128;
+        auto kernel = p->compensated ? k_gather_tiled<K, true, MODE> : k_gather_tiled<K, false, MODE>;
+        cudaError_t e = prepare_smem(kernel, smem);
+        if (e != cudaSuccess) return e;
+        int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kThreads, smem);
+        if (blocks > p->n_chunks) blocks = static_cast<int>(p->n_chunks);
+        kernel<<<blocks, kThreads, smem, p->stream>>>(p->tmap, static_cast<const Rec32 *>(p->recs), p->chunks,
+                                                      static_cast<float2 *>(f), static_cast<const float2 *>(v),
+                                                      static_cast<float *>(g1), static_cast<float *>(g2), a);
+        return cudaGetLastError();
+    }
+    const int blocks = static_cast<int>((p->M + kThreads - 1) / kThreads);
+    if (blocks == 0) return cudaSuccess;
+    if (p->precision == NFFT2D_F64) {
+        k_gather_direct<K, double, Rec64, MODE><<<blocks, kThreads, 0, p->stream>>>(
+            static_cast<const double2 *>(p->grid), static_cast<const Rec64 *>(p->recs), static_cast<double2 *>(f),
+            static_cast<const double2 *>(v), static_cast<double *>(g1), static_cast<double *>(g2), a);
+    } else {
+        k_gather_direct<K, float, Rec32, MODE><<<blocks, kThreads, 0, p->stream>>>(
+            static_cast<const float2 *>(p->grid), static_cast<const Rec32 *>(p->recs), static_cast<float2 *>(f),
+            static_cast<const float2 *>(v), static_cast<float *>(g1), static_cast<float *>(g2), a);
+    }
+    return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t dispatch(const nfft2d_plan_s *p, void *f, const void *v, void *g1, void *g2) {
+    switch (p->K) {
+        case 2: return launch_K<2, MODE>(p, f, v, g1, g2);
+        case 3: return launch_K<3, MODE>(p, f, v, g1, g2);
+        case 4: return launch_K<4, MODE>(p, f, v, g1, g2);
+        case 5: return launch_K<5, MODE>(p, f, v, g1, g2);
+        case 6: return launch_K<6, MODE>(p, f, v, g1, g2);
+        case 7: return launch_K<7, MODE>(p, f, v, g1, g2);
+        case 8: return launch_K<8, MODE>(p, f, v, g1, g2);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_gather(const nfft2d_plan_s *p, void *f) { return dispatch<0>(p, f, nullptr, nullptr, nullptr); }
+
+cudaError_t launch_grad(const nfft2d_plan_s *p, const void *v, void *g1, void *g2) {
+    return dispatch<1>(p, nullptr, v, g1, g2);
+}
+
+int gather_smem_bytes(const nfft2d_plan_s *p) { return 2 * patch_stride_elems(p->g) * static_cast<int>(sizeof(float2)) + 128; }
+
+}  // namespace nfft2d

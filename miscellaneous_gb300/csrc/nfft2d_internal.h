@@ -1,0 +1,136 @@
+// nfft2d_internal.h -- plan object and launcher declarations shared by the
+// translation units of libnfft2d_gb300.so (host side, C++17).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include "../../include/nfft2d_gb300.h"
+
+namespace nfft2d {
+
+constexpr int kHalo = 8;          // periodic halo around the oversampled grid (>= K rounded up to even)
+constexpr int kMinK = 2;
+constexpr int kMaxK = 8;
+constexpr unsigned kInvalidKey = 0xFFFFFFFFu;
+
+// Device-side error bits latched in Plan::d_status[1].
+constexpr int kErrTimeout = 1;
+constexpr int kErrBounds = 2;
+constexpr int kErrNonfinite = 4;
+
+// One binned point, FP32 plans: fractional offsets t = sigma*x_grid - mu in
+// [-1/2, 1/2], packed wrapped cell (mu1 << 16 | mu2) and the caller's index.
+struct __align__(16) Rec32 {
+    float t1, t2;
+    int mu;
+    int orig;
+};
+// FP64 plans keep the offsets in double.
+struct __align__(8) Rec64 {
+    double t1, t2;
+    int mu;
+    int orig;
+};
+
+// Window constants of one plan (both precisions are filled).
+struct WinConst {
+    double alpha;   // (2 - 1/sigma) pi - 0.01  (NFFT1_2D.m:11, NFFT2_2D.cu:27)
+    double cn;      // K / sinh(alpha K): normalises phi_hat to 1 at t = 0
+    double kp;      // K / (1 - exp(-2 alpha K)) = cn * exp(alpha K) / 2
+};
+
+// Geometry shared by kernels.
+struct Geom {
+    int n1, n2;         // oversampled grid
+    int H;              // halo
+    int R, C;           // padded grid: logical rows n1+2H, row pitch tiles2*T+2H (complex elements)
+    int Ra;             // allocated rows tiles1*T+2H: every tile patch box lies inside the allocation
+    int Cl;             // logical columns n2+2H
+    int T;              // tile edge
+    int tiles1, tiles2;
+    int PR, PC;         // patch rows / cols (complex elements)
+    int Ke;             // K rounded up to even (column halo of a patch)
+};
+
+// Per-stage CUDA events on the plan's stream: ev[2s], ev[2s+1] bracket stage s.
+constexpr int kStages = 9;
+struct Timer {
+    bool on = false;
+    cudaEvent_t ev[2 * kStages] = {};
+    bool used[kStages] = {};
+};
+
+}  // namespace nfft2d
+
+struct nfft2d_plan_s {
+    int N1 = 0, N2 = 0, K = 0, precision = 0;
+    double sigma = 2.0;
+    nfft2d::Geom g{};
+    nfft2d::WinConst w{};
+    int chunk = 256;
+    int gather_variant = NFFT2D_VARIANT_TILED;
+    int spread_variant = NFFT2D_VARIANT_TILED;
+    int compensated = 1;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+
+    // device buffers owned by the plan
+    void *grid = nullptr;        // R*C complex, the padded oversampled grid
+    void *deap1 = nullptr;       // N1 reals: S / phi(xi_k1), plan precision
+    void *deap2 = nullptr;       // N2 reals
+    int *d_status = nullptr;     // [0] n_chunks, [1] error bits
+    unsigned *cell_count = nullptr;  // ncells + 1 counters / starts
+    size_t ncells = 0;
+    unsigned *tile_chunks = nullptr; // ntiles + 1
+    unsigned *scan_tmp = nullptr;
+    size_t scan_tmp_elems = 0;
+
+    // points
+    long long M = 0;             // points set (0: none)
+    bool points_valid = false;
+    long long capM = 0;
+    void *recs = nullptr;        // sorted Rec32/Rec64
+    void *tmp_recs = nullptr;    // unsorted records, key in .orig
+    unsigned *ranks = nullptr;
+    int4 *chunks = nullptr;
+    long long chunks_cap = 0;
+    long long n_chunks = 0;
+    double xscale1 = 1.0, xscale2 = 1.0;  // dt/dx for the units given to set_points
+
+    cufftHandle fft = 0;
+    bool fft_ok = false;
+    CUtensorMap tmap;  // 64-byte aligned by its own declaration
+    bool tmap_ok = false;
+
+    nfft2d::Timer timer;
+    nfft2d_timings last{};
+    size_t workspace_bytes = 0;
+};
+
+namespace nfft2d {
+
+// ---- launchers (defined in the .cu files) --------------------------------
+// plan.cu
+cudaError_t launch_pad(const nfft2d_plan_s *p, const void *F);
+cudaError_t launch_crop(const nfft2d_plan_s *p, void *F);
+cudaError_t launch_halo_fill(const nfft2d_plan_s *p);
+cudaError_t launch_halo_fold(const nfft2d_plan_s *p);
+
+// gather.cu
+cudaError_t launch_gather(const nfft2d_plan_s *p, void *f);
+cudaError_t launch_grad(const nfft2d_plan_s *p, const void *v, void *g1, void *g2);
+int gather_smem_bytes(const nfft2d_plan_s *p);
+
+// spread.cu
+cudaError_t launch_spread(const nfft2d_plan_s *p, const void *f);
+
+// Geometry for given parameters; returns NFFT2D_OK or an error status.
+int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1, int *n2);
+
+int grid_blocks(const nfft2d_plan_s *p, const void *kernel, int threads, int smem);
+
+}  // namespace nfft2d

@@ -1,0 +1,1078 @@
+// nfft2d_plan.cu -- plan life cycle, point binning (counting sort by tile and
+// cell), the small grid kernels (deapodize+pad, halo fill/fold, crop+deapodize)
+// and the C ABI entry points of libnfft2d_gb300.so.
+//
+// Reference path being replaced: NFFT/NFFT2_2D.cu:329-495 (NFFT2_2D_GPU:
+// constants, Kernel_Bessel, malloc/memset, Interpolation_NFFT2_2D_GPUKernel,
+// fftshift_2D + cufftExecC2C + fftshift_2D, Decimation_and_Scaling) and
+// BP_FBP_FFBP/NFFT1_2D.m:1-69 (deapodize + zero-pad, fft2, gather).
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "nfft2d_device.cuh"
+#include "nfft2d_internal.h"
+
+using namespace nfft2d;
+
+namespace {
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// ---------------------------------------------------------------------------
+// host math (plan time, FP64)
+// ---------------------------------------------------------------------------
+
+// I0 by its power series (Abramowitz & Stegun 9.6.12); all terms positive.
+double host_bessel_i0(double x) {
+    const double q = 0.25 * x * x;
+    double term = 1.0, sum = 1.0;
+    for (int j = 1; j < 500; ++j) {
+        term *= q / (static_cast<double>(j) * j);
+        sum += term;
+        if (term < 1e-18 * sum) break;
+    }
+    return sum;
+}
+
+int status_from_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return NFFT2D_OK;
+    if (e == cudaErrorMemoryAllocation) return NFFT2D_ERR_OOM;
+    return NFFT2D_ERR_CUDA;
+}
+
+int status_from_cufft(cufftResult r) {
+    if (r == CUFFT_SUCCESS) return NFFT2D_OK;
+    if (r == CUFFT_ALLOC_FAILED) return NFFT2D_ERR_OOM;
+    return NFFT2D_ERR_CUFFT;
+}
+
+#define NFFT_TRY_CUDA(expr)                                  \
+    do {                                                     \
+        cudaError_t e_ = (expr);                             \
+        if (e_ != cudaSuccess) return status_from_cuda(e_);  \
+    } while (0)
+
+size_t real_size(int precision) { return precision == NFFT2D_F64 ? sizeof(double) : sizeof(float); }
+size_t cplx_size(int precision) { return 2 * real_size(precision); }
+size_t rec_size(int precision) { return precision == NFFT2D_F64 ? sizeof(Rec64) : sizeof(Rec32); }
+
+// ---------------------------------------------------------------------------
+// stage timing
+// ---------------------------------------------------------------------------
+enum Stage { ST_SORT = 0, ST_PAD, ST_FFT2, ST_FILL, ST_GATHER, ST_SPREAD, ST_FOLD, ST_FFT1, ST_CROP, ST_COUNT };
+static_assert(ST_COUNT == kStages, "stage count");
+
+void stage_begin(nfft2d_plan_s *p, Stage s) {
+    if (!p->timer.on) return;
+    cudaEventRecord(p->timer.ev[2 * s], p->stream);
+    p->timer.used[s] = true;
+}
+void stage_end(nfft2d_plan_s *p, Stage s) {
+    if (!p->timer.on) return;
+    cudaEventRecord(p->timer.ev[2 * s + 1], p->stream);
+}
+// Forget the stages a call of this kind is about to re-run.
+enum CallKind { CALL_SORT, CALL_TYPE2, CALL_TYPE1 };
+void timer_reset(nfft2d_plan_s *p, CallKind k) {
+    static const Stage sort_st[] = {ST_SORT};
+    static const Stage t2_st[] = {ST_PAD, ST_FFT2, ST_FILL, ST_GATHER};
+    static const Stage t1_st[] = {ST_SPREAD, ST_FOLD, ST_FFT1, ST_CROP};
+    if (k == CALL_SORT) for (Stage s : sort_st) p->timer.used[s] = false;
+    if (k == CALL_TYPE2) for (Stage s : t2_st) p->timer.used[s] = false;
+    if (k == CALL_TYPE1) for (Stage s : t1_st) p->timer.used[s] = false;
+}
+
+// ---------------------------------------------------------------------------
+// TMA descriptor (driver entry point fetched through the runtime, so the
+// library does not link libcuda directly)
+// ---------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    }
+    return fn;
+}
+
+// The padded grid seen as a 2D FP32 tensor: Ra rows, 2*C floats per row.  One
+// box is a tile patch: PR rows x 2*PC floats; the allocation is a whole number
+// of tiles plus the halo on each side, so every box lies inside it.
+int make_tensor_map(nfft2d_plan_s *p) {
+    EncodeTiledFn enc = get_encode_tiled();
+    if (!enc) return NFFT2D_ERR_CUDA;
+    const Geom &g = p->g;
+    cuuint64_t dims[2] = {static_cast<cuuint64_t>(2 * g.C), static_cast<cuuint64_t>(g.Ra)};
+    cuuint64_t strides[1] = {static_cast<cuuint64_t>(2 * g.C) * sizeof(float)};
+    cuuint32_t box[2] = {static_cast<cuuint32_t>(2 * g.PC), static_cast<cuuint32_t>(g.PR)};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, p->grid, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return NFFT2D_ERR_CUDA;
+    p->tmap_ok = true;
+    return NFFT2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device kernels: deapodize + zero-pad, crop + deapodize, halo fill / fold
+// ---------------------------------------------------------------------------
+template <typename Cx, typename Rl>
+__global__ void k_pad(const Cx *__restrict__ F, Cx *__restrict__ grid, const Rl *__restrict__ d1,
+                      const Rl *__restrict__ d2, int N1, int N2, int n1, int n2, int H, int C) {
+    // One row r of the oversampled grid per blockIdx.y.  FFT index r holds
+    // frequency k1 = r (r < n1/2) or r - n1: the ifftshift of NFFT1_2D.m:55
+    // applied to the centered zero-padded block of NFFT1_2D.m:48-49.
+    const int r = blockIdx.y;
+    const int k1 = (r < n1 / 2) ? r : r - n1;
+    const bool row_in = (k1 >= -N1 / 2) && (k1 < N1 / 2);
+    const int i = k1 + N1 / 2;
+    const Rl s1 = row_in ? d1[i] : Rl(0);
+    Cx *dst = grid + static_cast<size_t>(r + H) * C + H;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n2; c += gridDim.x * blockDim.x) {
+        const int k2 = (c < n2 / 2) ? c : c - n2;
+        Cx v;
+        v.x = Rl(0);
+        v.y = Rl(0);
+        if (row_in && k2 >= -N2 / 2 && k2 < N2 / 2) {
+            const int j = k2 + N2 / 2;
+            const Rl s = s1 * d2[j];
+            const Cx f = F[static_cast<size_t>(i) * N2 + j];
+            v.x = f.x * s;
+            v.y = f.y * s;
+        }
+        dst[c] = v;
+    }
+}
+
+template <typename Cx, typename Rl>
+__global__ void k_crop(const Cx *__restrict__ grid, Cx *__restrict__ F, const Rl *__restrict__ d1,
+                       const Rl *__restrict__ d2, int N1, int N2, int n1, int n2, int H, int C) {
+    // Decimation_and_Scaling (NFFT2_2D.cu:74-100, NFFT2_2D.m:70): keep
+    // frequencies [-N/2, N/2) and multiply by the deapodization table.  The
+    // fftshift pair around the FFT (NFFT2_2D.cu:383,393) is folded into the
+    // index map k -> k mod n.
+    const int i = blockIdx.y;
+    const int k1 = i - N1 / 2;
+    const int r = k1 < 0 ? k1 + n1 : k1;
+    const Rl s1 = d1[i];
+    const Cx *src = grid + static_cast<size_t>(r + H) * C + H;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N2; j += gridDim.x * blockDim.x) {
+        const int k2 = j - N2 / 2;
+        const int c = k2 < 0 ? k2 + n2 : k2;
+        const Rl s = s1 * d2[j];
+        const Cx g = src[c];
+        Cx v;
+        v.x = g.x * s;
+        v.y = g.y * s;
+        F[static_cast<size_t>(i) * N2 + j] = v;
+    }
+}
+
+__device__ __forceinline__ int pmod(int a, int n) {
+    int r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+// Fill the periodic halo of the padded grid from the interior (type 2, after
+// the FFT), so a tile patch never needs index wrapping.
+template <typename Cx>
+__global__ void k_halo_fill(Cx *__restrict__ grid, int n1, int n2, int H, int C) {
+    const long long top = 2LL * H * C;
+    const long long side = 2LL * H * n1;
+    for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < top + side;
+         idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int r, c;
+        if (idx < top) {
+            const int rr = static_cast<int>(idx / C);
+            c = static_cast<int>(idx - static_cast<long long>(rr) * C);
+            r = rr < H ? rr : rr + n1;
+        } else {
+            const long long j = idx - top;
+            r = H + static_cast<int>(j / (2 * H));
+            const int cc = static_cast<int>(j - static_cast<long long>(r - H) * 2 * H);
+            c = cc < H ? cc : cc + n2;
+        }
+        const int sr = pmod(r - H, n1) + H, sc = pmod(c - H, n2) + H;
+        grid[static_cast<size_t>(r) * C + c] = grid[static_cast<size_t>(sr) * C + sc];
+    }
+}
+
+// Fold the halo back onto the interior (type 1, after spreading): every
+// interior cell within H of an edge adds all of its periodic images that lie
+// in the padded grid.  Each such cell is owned by one thread; halo cells are
+// only read, so no atomics are needed.
+template <typename Cx>
+__global__ void k_halo_fold(Cx *__restrict__ grid, int n1, int n2, int H, int R, int Cl, int C) {
+    const int rows_tb = (n1 <= 2 * H) ? n1 : 2 * H;
+    const int cols_lr = (n2 <= 2 * H) ? n2 : 2 * H;
+    const long long part1 = static_cast<long long>(rows_tb) * n2;
+    const long long part2 = (n1 > 2 * H) ? static_cast<long long>(n1 - 2 * H) * cols_lr : 0;
+    for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < part1 + part2;
+         idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int r, c;
+        if (idx < part1) {
+            const int rr = static_cast<int>(idx / n2);
+            c = static_cast<int>(idx - static_cast<long long>(rr) * n2);
+            r = (n1 <= 2 * H) ? rr : (rr < H ? rr : n1 - 2 * H + rr);
+        } else {
+            const long long j = idx - part1;
+            const int rr = static_cast<int>(j / cols_lr);
+            const int cc = static_cast<int>(j - static_cast<long long>(rr) * cols_lr);
+            r = H + rr;
+            c = (n2 <= 2 * H) ? cc : (cc < H ? cc : n2 - 2 * H + cc);
+        }
+        // images at padded (r + H + a*n1, c + H + b*n2), (a, b) != (0, 0)
+        const int pr0 = r + H, pc0 = c + H;
+        const int amin = -((pr0) / n1), amax = (R - 1 - pr0) / n1;
+        const int bmin = -((pc0) / n2), bmax = (Cl - 1 - pc0) / n2;
+        auto acc = grid[static_cast<size_t>(pr0) * C + pc0];
+        for (int a = amin; a <= amax; ++a)
+            for (int b = bmin; b <= bmax; ++b) {
+                if (a == 0 && b == 0) continue;
+                const auto v = grid[static_cast<size_t>(pr0 + a * n1) * C + (pc0 + b * n2)];
+                acc.x += v.x;
+                acc.y += v.y;
+            }
+        grid[static_cast<size_t>(pr0) * C + pc0] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// binning: per point cell key, counting sort by key, work items per tile
+// ---------------------------------------------------------------------------
+template <typename CT, typename RecT>
+__global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double s1, double s2,
+                            Geom g, RecT *__restrict__ tmp, unsigned *__restrict__ ranks,
+                            unsigned *__restrict__ cell_count, int *__restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    // FP64 coordinate reduction: v = sigma * x_grid, mu = rint(v)
+    // (NFFT2_2D.cu:167-173 computes the same in the data precision).
+    const double v1 = static_cast<double>(x1[i]) * s1;
+    const double v2 = static_cast<double>(x2[i]) * s2;
+    if (!isfinite(v1) || !isfinite(v2)) {
+        latch_error(status, kErrNonfinite);
+        tmp[i].orig = static_cast<int>(kInvalidKey);
+        return;
+    }
+    const double m1 = rint(v1), m2 = rint(v2);
+    const double t1 = v1 - m1, t2 = v2 - m2;
+    double w1 = m1 - static_cast<double>(g.n1) * floor(m1 * (1.0 / g.n1));
+    double w2 = m2 - static_cast<double>(g.n2) * floor(m2 * (1.0 / g.n2));
+    if (w1 >= g.n1) w1 -= g.n1;
+    if (w1 < 0) w1 += g.n1;
+    if (w2 >= g.n2) w2 -= g.n2;
+    if (w2 < 0) w2 += g.n2;
+    const int mu1 = static_cast<int>(w1), mu2 = static_cast<int>(w2);
+    const int tr = mu1 / g.T, tc = mu2 / g.T;
+    const unsigned key = (static_cast<unsigned>(tr * g.tiles2 + tc) * g.T + (mu1 - tr * g.T)) * g.T + (mu2 - tc * g.T);
+    const unsigned rank = atomicAdd(cell_count + key, 1u);
+    RecT r;
+    r.t1 = static_cast<decltype(r.t1)>(t1);
+    r.t2 = static_cast<decltype(r.t2)>(t2);
+    r.mu = (mu1 << 16) | mu2;
+    r.orig = static_cast<int>(key);
+    tmp[i] = r;
+    ranks[i] = rank;
+}
+
+template <typename RecT>
+__global__ void k_bin_scatter(const RecT *__restrict__ tmp, const unsigned *__restrict__ ranks,
+                              const unsigned *__restrict__ cell_start, int M, RecT *__restrict__ recs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    RecT r = tmp[i];
+    const unsigned key = static_cast<unsigned>(r.orig);
+    if (key == kInvalidKey) return;
+    r.orig = i;
+    recs[cell_start[key] + ranks[i]] = r;
+}
+
+__global__ void k_tile_chunk_count(const unsigned *__restrict__ cell_start, int ntiles, int cells_per_tile, int chunk,
+                                   unsigned *__restrict__ tile_chunks) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntiles) return;
+    if (t == ntiles) {
+        tile_chunks[t] = 0;
+        return;
+    }
+    const unsigned a = cell_start[static_cast<size_t>(t) * cells_per_tile];
+    const unsigned b = cell_start[static_cast<size_t>(t + 1) * cells_per_tile];
+    tile_chunks[t] = (b - a + chunk - 1) / chunk;
+}
+
+__global__ void k_emit_chunks(const unsigned *__restrict__ cell_start, const unsigned *__restrict__ tile_chunks,
+                              int ntiles, int cells_per_tile, int chunk, int4 *__restrict__ chunks,
+                              int *__restrict__ status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    if (t == 0) status[0] = static_cast<int>(tile_chunks[ntiles]);
+    const unsigned base = tile_chunks[t];
+    const unsigned nch = tile_chunks[t + 1] - base;
+    const unsigned start = cell_start[static_cast<size_t>(t) * cells_per_tile];
+    const unsigned cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] - start;
+    for (unsigned c = 0; c < nch; ++c) {
+        const unsigned off = c * chunk;
+        chunks[base + c] = make_int4(t, static_cast<int>(start + off), static_cast<int>(min(cnt - off, (unsigned)chunk)), 0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of unsigned counters (3 phases, recursive on block sums)
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void k_scan_reduce(const unsigned *__restrict__ in, size_t n, unsigned *__restrict__ sums) {
+    __shared__ unsigned warp_sums[kScanThreads / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * kScanTile;
+    unsigned s = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        const size_t i = base + static_cast<size_t>(k) * kScanThreads + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned v = threadIdx.x < kScanThreads / 32 ? warp_sums[threadIdx.x] : 0u;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) sums[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_scan_apply(unsigned *__restrict__ data, size_t n, const unsigned *__restrict__ offsets) {
+    __shared__ unsigned warp_tot[kScanThreads / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * kScanTile + static_cast<size_t>(threadIdx.x) * kScanItems;
+    unsigned v[kScanItems];
+    unsigned tsum = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        const size_t i = base + k;
+        v[k] = i < n ? data[i] : 0u;
+        tsum += v[k];
+    }
+    // block-wide exclusive scan of thread totals
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned incl = tsum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned w = lane < kScanThreads / 32 ? warp_tot[lane] : 0u;
+        unsigned wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
+    }
+    __syncthreads();
+    unsigned run = (offsets ? offsets[blockIdx.x] : 0u) + warp_tot[wid] + (incl - tsum);
+    for (int k = 0; k < kScanItems; ++k) {
+        const size_t i = base + k;
+        if (i < n) data[i] = run;
+        run += v[k];
+    }
+}
+
+size_t scan_tmp_needed(size_t n) {
+    size_t total = 0;
+    while (n > static_cast<size_t>(kScanTile)) {
+        n = (n + kScanTile - 1) / kScanTile;
+        total += n;
+    }
+    return total + 64;
+}
+
+cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *tmp, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const size_t nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 1) {
+        k_scan_apply<<<1, kScanThreads, 0, st>>>(data, n, nullptr);
+        return cudaGetLastError();
+    }
+    k_scan_reduce<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(data, n, tmp);
+    cudaError_t e = exclusive_scan(tmp, nb, tmp + nb, st);
+    if (e != cudaSuccess) return e;
+    k_scan_apply<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(data, n, tmp);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// plan helpers
+// ---------------------------------------------------------------------------
+void free_points(nfft2d_plan_s *p) {
+    cudaFree(p->recs);
+    cudaFree(p->tmp_recs);
+    cudaFree(p->ranks);
+    cudaFree(p->chunks);
+    p->recs = p->tmp_recs = nullptr;
+    p->ranks = nullptr;
+    p->chunks = nullptr;
+    p->capM = 0;
+    p->chunks_cap = 0;
+}
+
+void destroy_plan(nfft2d_plan_s *p) {
+    if (!p) return;
+    if (p->fft_ok) cufftDestroy(p->fft);
+    free_points(p);
+    cudaFree(p->grid);
+    cudaFree(p->deap1);
+    cudaFree(p->deap2);
+    cudaFree(p->d_status);
+    cudaFree(p->cell_count);
+    cudaFree(p->tile_chunks);
+    cudaFree(p->scan_tmp);
+    for (auto &e : p->timer.ev)
+        if (e) cudaEventDestroy(e);
+    delete p;
+}
+
+long long chunks_capacity(const nfft2d_plan_s *p, long long M) {
+    return static_cast<long long>(p->g.tiles1) * p->g.tiles2 + M / p->chunk + 1;
+}
+
+int ensure_points_capacity(nfft2d_plan_s *p, long long M) {
+    const long long need_chunks = chunks_capacity(p, M);
+    if (M <= p->capM && need_chunks <= p->chunks_cap) return NFFT2D_OK;
+    free_points(p);
+    const long long cap = std::max<long long>(M, 1);
+    const size_t rs = rec_size(p->precision);
+    NFFT_TRY_CUDA(cudaMalloc(&p->recs, rs * cap));
+    NFFT_TRY_CUDA(cudaMalloc(&p->tmp_recs, rs * cap));
+    NFFT_TRY_CUDA(cudaMalloc(&p->ranks, sizeof(unsigned) * cap));
+    const long long cc = chunks_capacity(p, cap);
+    NFFT_TRY_CUDA(cudaMalloc(&p->chunks, sizeof(int4) * cc));
+    p->capM = cap;
+    p->chunks_cap = cc;
+    return NFFT2D_OK;
+}
+
+size_t plan_workspace_bytes(const nfft2d_plan_s *p) {
+    const size_t grid = cplx_size(p->precision) * static_cast<size_t>(p->g.Ra) * p->g.C;
+    const size_t pts = static_cast<size_t>(p->capM) * (2 * rec_size(p->precision) + sizeof(unsigned)) +
+                       static_cast<size_t>(p->chunks_cap) * sizeof(int4);
+    const size_t bins = sizeof(unsigned) * (p->ncells + 1 + p->g.tiles1 * p->g.tiles2 + 1 + p->scan_tmp_elems);
+    return grid + pts + bins + real_size(p->precision) * (p->N1 + p->N2);
+}
+
+int check_plan(nfft2d_plan_s *p) { return p ? NFFT2D_OK : NFFT2D_ERR_INVALID_ARG; }
+
+// (Re)allocate the padded grid for the current geometry, rebuild the cuFFT
+// plan on its interior (advanced layout) and the TMA descriptor.
+int setup_grid(nfft2d_plan_s *p) {
+    const Geom &g = p->g;
+    if (p->fft_ok) {
+        cufftDestroy(p->fft);
+        p->fft_ok = false;
+    }
+    cudaFree(p->grid);
+    p->grid = nullptr;
+    p->tmap_ok = false;
+    const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C;
+    NFFT_TRY_CUDA(cudaMalloc(&p->grid, bytes));
+    NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, bytes, p->stream));
+    int n[2] = {g.n1, g.n2};
+    int emb[2] = {g.Ra, g.C};
+    const int dist = g.Ra * g.C;
+    cufftResult fr = cufftPlanMany(&p->fft, 2, n, emb, 1, dist, emb, 1, dist,
+                                   p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C, 1);
+    if (fr != CUFFT_SUCCESS) return status_from_cufft(fr);
+    p->fft_ok = true;
+    if ((fr = cufftSetStream(p->fft, p->stream)) != CUFFT_SUCCESS) return status_from_cufft(fr);
+    if (p->precision == NFFT2D_F32) return make_tensor_map(p);
+    return NFFT2D_OK;
+}
+
+// (Re)allocate the bin counters for the current tile geometry.
+int setup_bins(nfft2d_plan_s *p) {
+    const Geom &g = p->g;
+    cudaFree(p->cell_count);
+    cudaFree(p->tile_chunks);
+    cudaFree(p->scan_tmp);
+    p->cell_count = p->tile_chunks = p->scan_tmp = nullptr;
+    p->ncells = static_cast<size_t>(g.tiles1) * g.tiles2 * g.T * g.T;
+    const int ntiles = g.tiles1 * g.tiles2;
+    p->scan_tmp_elems = std::max(scan_tmp_needed(p->ncells + 1), scan_tmp_needed(ntiles + 1));
+    NFFT_TRY_CUDA(cudaMalloc(&p->cell_count, sizeof(unsigned) * (p->ncells + 1)));
+    NFFT_TRY_CUDA(cudaMalloc(&p->tile_chunks, sizeof(unsigned) * (ntiles + 1)));
+    NFFT_TRY_CUDA(cudaMalloc(&p->scan_tmp, sizeof(unsigned) * p->scan_tmp_elems));
+    return NFFT2D_OK;
+}
+
+
+// Launch shape for the small elementwise kernels.
+dim3 row_grid(int cols, int rows) {
+    const int bx = std::max(1, std::min((cols + 255) / 256, 64));
+    return dim3(bx, rows, 1);
+}
+
+}  // namespace
+
+// ===========================================================================
+// internal API used by the other translation units
+// ===========================================================================
+namespace nfft2d {
+
+int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1o, int *n2o) {
+    if (N1 <= 0 || N2 <= 0 || (N1 & 1) || (N2 & 1)) return NFFT2D_ERR_INVALID_ARG;
+    if (K < kMinK || K > kMaxK) return NFFT2D_ERR_INVALID_ARG;
+    if (precision != NFFT2D_F32 && precision != NFFT2D_F64) return NFFT2D_ERR_INVALID_ARG;
+    if (!(sigma >= 1.25) || !std::isfinite(sigma)) return NFFT2D_ERR_INVALID_ARG;
+    const double c1 = sigma * N1, c2 = sigma * N2;
+    const long long n1 = std::llround(c1), n2 = std::llround(c2);
+    if (std::fabs(c1 - n1) > 1e-9 || std::fabs(c2 - n2) > 1e-9) return NFFT2D_ERR_INVALID_ARG;
+    if ((n1 & 1) || (n2 & 1)) return NFFT2D_ERR_INVALID_ARG;
+    if (n1 < 2 * K + 2 || n2 < 2 * K + 2) return NFFT2D_ERR_INVALID_ARG;
+    if (n1 > 46000 || n2 > 46000) return NFFT2D_ERR_INVALID_ARG;
+    const int nmin = static_cast<int>(std::min(n1, n2));
+    int T = tile;
+    if (T == 0) {
+        T = 32;
+        while (T > 8 && T > nmin) T >>= 1;
+    }
+    if (T != 8 && T != 16 && T != 32 && T != 64) return NFFT2D_ERR_INVALID_ARG;
+    if (T > nmin) return NFFT2D_ERR_INVALID_ARG;
+    g->n1 = static_cast<int>(n1);
+    g->n2 = static_cast<int>(n2);
+    g->H = kHalo;
+    g->T = T;
+    g->tiles1 = (g->n1 + T - 1) / T;
+    g->tiles2 = (g->n2 + T - 1) / T;
+    g->R = g->n1 + 2 * kHalo;
+    g->Cl = g->n2 + 2 * kHalo;
+    g->C = g->tiles2 * T + 2 * kHalo;
+    g->Ra = g->tiles1 * T + 2 * kHalo;
+    g->Ke = K + (K & 1);
+    g->PR = T + 2 * K;
+    g->PC = T + 2 * g->Ke;
+    const unsigned long long ncells = 1ULL * g->tiles1 * g->tiles2 * T * T;
+    if (ncells >= (1ULL << 31)) return NFFT2D_ERR_INVALID_ARG;
+    if (n1o) *n1o = g->n1;
+    if (n2o) *n2o = g->n2;
+    return NFFT2D_OK;
+}
+
+int grid_blocks(const nfft2d_plan_s *p, const void *kernel, int threads, int smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * std::max(1, p->num_sms);
+}
+
+cudaError_t launch_pad(const nfft2d_plan_s *p, const void *F) {
+    const Geom &g = p->g;
+    const dim3 grid = row_grid(g.n2, g.n1);
+    if (p->precision == NFFT2D_F64)
+        k_pad<double2, double><<<grid, 256, 0, p->stream>>>(
+            static_cast<const double2 *>(F), static_cast<double2 *>(p->grid), static_cast<const double *>(p->deap1),
+            static_cast<const double *>(p->deap2), p->N1, p->N2, g.n1, g.n2, g.H, g.C);
+    else
+        k_pad<float2, float><<<grid, 256, 0, p->stream>>>(
+            static_cast<const float2 *>(F), static_cast<float2 *>(p->grid), static_cast<const float *>(p->deap1),
+            static_cast<const float *>(p->deap2), p->N1, p->N2, g.n1, g.n2, g.H, g.C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crop(const nfft2d_plan_s *p, void *F) {
+    const Geom &g = p->g;
+    const dim3 grid = row_grid(p->N2, p->N1);
+    if (p->precision == NFFT2D_F64)
+        k_crop<double2, double><<<grid, 256, 0, p->stream>>>(
+            static_cast<const double2 *>(p->grid), static_cast<double2 *>(F), static_cast<const double *>(p->deap1),
+            static_cast<const double *>(p->deap2), p->N1, p->N2, g.n1, g.n2, g.H, g.C);
+    else
+        k_crop<float2, float><<<grid, 256, 0, p->stream>>>(
+            static_cast<const float2 *>(p->grid), static_cast<float2 *>(F), static_cast<const float *>(p->deap1),
+            static_cast<const float *>(p->deap2), p->N1, p->N2, g.n1, g.n2, g.H, g.C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_halo_fill(const nfft2d_plan_s *p) {
+    const Geom &g = p->g;
+    const long long n = 2LL * g.H * g.C + 2LL * g.H * g.n1;
+    const int blocks = static_cast<int>(std::min<long long>((n + 255) / 256, 4LL * p->num_sms));
+    if (p->precision == NFFT2D_F64)
+        k_halo_fill<double2><<<blocks, 256, 0, p->stream>>>(static_cast<double2 *>(p->grid), g.n1, g.n2, g.H, g.C);
+    else
+        k_halo_fill<float2><<<blocks, 256, 0, p->stream>>>(static_cast<float2 *>(p->grid), g.n1, g.n2, g.H, g.C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_halo_fold(const nfft2d_plan_s *p) {
+    const Geom &g = p->g;
+    const long long n = 2LL * g.H * (g.n1 + g.n2);
+    const int blocks = static_cast<int>(std::min<long long>((n + 255) / 256, 4LL * p->num_sms));
+    if (p->precision == NFFT2D_F64)
+        k_halo_fold<double2><<<blocks, 256, 0, p->stream>>>(static_cast<double2 *>(p->grid), g.n1, g.n2, g.H, g.R, g.Cl, g.C);
+    else
+        k_halo_fold<float2><<<blocks, 256, 0, p->stream>>>(static_cast<float2 *>(p->grid), g.n1, g.n2, g.H, g.R, g.Cl, g.C);
+    return cudaGetLastError();
+}
+
+}  // namespace nfft2d
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+namespace {
+
+int run_fft(nfft2d_plan_s *p, int sign) {
+    const Geom &g = p->g;
+    const int dir = sign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
+    const size_t off = static_cast<size_t>(g.H) * g.C + g.H;
+    cufftResult r;
+    if (p->precision == NFFT2D_F64) {
+        cufftDoubleComplex *d = static_cast<cufftDoubleComplex *>(p->grid) + off;
+        r = cufftExecZ2Z(p->fft, d, d, dir);
+    } else {
+        cufftComplex *d = static_cast<cufftComplex *>(p->grid) + off;
+        r = cufftExecC2C(p->fft, d, d, dir);
+    }
+    return status_from_cufft(r);
+}
+
+int type2_prepare(nfft2d_plan_s *p, int sign, const void *F) {
+    stage_begin(p, ST_PAD);
+    NFFT_TRY_CUDA(launch_pad(p, F));
+    stage_end(p, ST_PAD);
+    stage_begin(p, ST_FFT2);
+    int st = run_fft(p, sign);
+    if (st != NFFT2D_OK) return st;
+    stage_end(p, ST_FFT2);
+    stage_begin(p, ST_FILL);
+    NFFT_TRY_CUDA(launch_halo_fill(p));
+    stage_end(p, ST_FILL);
+    return NFFT2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *nfft2d_status_string(int s) {
+    switch (s) {
+        case NFFT2D_OK: return "ok";
+        case NFFT2D_ERR_INVALID_ARG: return "invalid argument";
+        case NFFT2D_ERR_OOM: return "out of memory";
+        case NFFT2D_ERR_CUDA: return "CUDA runtime error";
+        case NFFT2D_ERR_CUFFT: return "cuFFT error";
+        case NFFT2D_ERR_NO_POINTS: return "no points set on the plan";
+        case NFFT2D_ERR_NONFINITE: return "non-finite point coordinate";
+        case NFFT2D_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+        case NFFT2D_ERR_DEVICE_BOUNDS: return "device-side bounds check failed";
+        case NFFT2D_ERR_UNSUPPORTED: return "unsupported request";
+        case NFFT2D_ERR_INTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+int nfft2d_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+int nfft2d_layout_query(int N1, int N2, double sigma, int K, int precision, int tile, nfft2d_info *info) {
+    if (!info) return NFFT2D_ERR_INVALID_ARG;
+    Geom g{};
+    int st = compute_layout(N1, N2, sigma, K, precision, tile, &g, nullptr, nullptr);
+    if (st != NFFT2D_OK) return st;
+    std::memset(info, 0, sizeof(*info));
+    info->N1 = N1;
+    info->N2 = N2;
+    info->sigma = sigma;
+    info->K = K;
+    info->precision = precision;
+    info->n1 = g.n1;
+    info->n2 = g.n2;
+    info->halo = g.H;
+    info->rows = g.Ra;
+    info->cols = g.C;
+    info->tile = g.T;
+    info->tiles1 = g.tiles1;
+    info->tiles2 = g.tiles2;
+    info->patch_rows = g.PR;
+    info->patch_cols = g.PC;
+    info->chunk = 256;
+    info->gather_variant = precision == NFFT2D_F32 ? NFFT2D_VARIANT_TILED : NFFT2D_VARIANT_DIRECT;
+    info->spread_variant = info->gather_variant;
+    return NFFT2D_OK;
+}
+
+int nfft2d_plan_create(nfft2d_plan *out, int N1, int N2, double sigma, int K, int precision, void *stream) {
+    if (!out) return NFFT2D_ERR_INVALID_ARG;
+    *out = nullptr;
+    Geom g{};
+    int st = compute_layout(N1, N2, sigma, K, precision, 0, &g, nullptr, nullptr);
+    if (st != NFFT2D_OK) return st;
+    nfft2d_plan_s *p = new (std::nothrow) nfft2d_plan_s();
+    if (!p) return NFFT2D_ERR_OOM;
+    p->N1 = N1;
+    p->N2 = N2;
+    p->K = K;
+    p->sigma = sigma;
+    p->precision = precision;
+    p->g = g;
+    p->stream = static_cast<cudaStream_t>(stream);
+    if (precision == NFFT2D_F64) {
+        p->gather_variant = NFFT2D_VARIANT_DIRECT;
+        p->spread_variant = NFFT2D_VARIANT_DIRECT;
+    }
+    auto fail = [&](int s) {
+        destroy_plan(p);
+        return s;
+    };
+    if (cudaGetDevice(&p->device) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    if (cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
+        return fail(NFFT2D_ERR_CUDA);
+
+    // window constants (FP64, plan time)
+    const double alpha = (2.0 - 1.0 / sigma) * kPi - 0.01;
+    p->w.alpha = alpha;
+    p->w.cn = K / std::sinh(alpha * K);
+    p->w.kp = K / (1.0 - std::exp(-2.0 * alpha * K));
+
+    const size_t rs = real_size(precision);
+    cudaError_t e;
+    if ((st = setup_grid(p)) != NFFT2D_OK) return fail(st);
+    if ((st = setup_bins(p)) != NFFT2D_OK) return fail(st);
+    if ((e = cudaMalloc(&p->deap1, rs * N1)) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = cudaMalloc(&p->deap2, rs * N2)) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = cudaMalloc(&p->d_status, 4 * sizeof(int))) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = cudaMemsetAsync(p->d_status, 0, 4 * sizeof(int), p->stream)) != cudaSuccess)
+        return fail(status_from_cuda(e));
+
+    // Deapodization tables S / phi(xi_k), S = sinh(alpha K)/(pi K) (the
+    // window normalisation), phi(xi) = I0(K sqrt(alpha^2 - xi^2)),
+    // xi_k = 2 pi k / (sigma N)  (NFFT1_2D.m:17-22, NFFT2_2D.cu:60-69).
+    const double S = std::sinh(alpha * K) / (kPi * K);
+    for (int d = 0; d < 2; ++d) {
+        const int N = d == 0 ? N1 : N2;
+        const double n = d == 0 ? g.n1 : g.n2;
+        std::vector<double> tab(N);
+        for (int i = 0; i < N; ++i) {
+            const double xi = 2.0 * kPi * (i - N / 2) / n;
+            tab[i] = S / host_bessel_i0(K * std::sqrt(alpha * alpha - xi * xi));
+        }
+        void *dst = d == 0 ? p->deap1 : p->deap2;
+        if (precision == NFFT2D_F64) {
+            e = cudaMemcpy(dst, tab.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+        } else {
+            std::vector<float> tf(tab.begin(), tab.end());
+            e = cudaMemcpy(dst, tf.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
+        }
+        if (e != cudaSuccess) return fail(status_from_cuda(e));
+    }
+
+    for (auto &ev : p->timer.ev)
+        if (cudaEventCreate(&ev) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return fail(status_from_cuda(e));
+    p->workspace_bytes = plan_workspace_bytes(p);
+    *out = p;
+    return NFFT2D_OK;
+}
+
+int nfft2d_plan_destroy(nfft2d_plan p) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    cudaStreamSynchronize(p->stream);
+    destroy_plan(p);
+    return NFFT2D_OK;
+}
+
+int nfft2d_set_stream(nfft2d_plan p, void *stream) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    p->stream = static_cast<cudaStream_t>(stream);
+    return status_from_cufft(cufftSetStream(p->fft, p->stream));
+}
+
+int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
+    if (!p || !t) return NFFT2D_ERR_INVALID_ARG;
+    if (t->tile != 0 && t->tile != p->g.T) {
+        Geom g{};
+        int st = compute_layout(p->N1, p->N2, p->sigma, p->K, p->precision, t->tile, &g, nullptr, nullptr);
+        if (st != NFFT2D_OK) return st;
+        cudaStreamSynchronize(p->stream);
+        p->g = g;
+        free_points(p);
+        p->points_valid = false;
+        p->M = 0;
+        if ((st = setup_grid(p)) != NFFT2D_OK) return st;
+        if ((st = setup_bins(p)) != NFFT2D_OK) return st;
+    }
+    if (t->chunk != 0) {
+        if (t->chunk < 32 || t->chunk > (1 << 20)) return NFFT2D_ERR_INVALID_ARG;
+        if (t->chunk != p->chunk) {
+            p->chunk = t->chunk;
+            p->points_valid = false;
+            p->M = 0;
+        }
+    }
+    for (int v : {t->gather_variant, t->spread_variant})
+        if (v < NFFT2D_VARIANT_AUTO || v > NFFT2D_VARIANT_DIRECT) return NFFT2D_ERR_INVALID_ARG;
+    const int auto_v = p->precision == NFFT2D_F32 ? NFFT2D_VARIANT_TILED : NFFT2D_VARIANT_DIRECT;
+    const int gv = t->gather_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->gather_variant;
+    const int sv = t->spread_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->spread_variant;
+    if (p->precision == NFFT2D_F64 && (gv == NFFT2D_VARIANT_TILED || sv == NFFT2D_VARIANT_TILED))
+        return NFFT2D_ERR_UNSUPPORTED;
+    p->gather_variant = gv;
+    p->spread_variant = sv;
+    if (t->compensated >= 0) p->compensated = t->compensated ? 1 : 0;
+    p->workspace_bytes = plan_workspace_bytes(p);
+    return NFFT2D_OK;
+}
+
+int nfft2d_get_info(nfft2d_plan p, nfft2d_info *info) {
+    if (!p || !info) return NFFT2D_ERR_INVALID_ARG;
+    std::memset(info, 0, sizeof(*info));
+    info->N1 = p->N1;
+    info->N2 = p->N2;
+    info->sigma = p->sigma;
+    info->K = p->K;
+    info->precision = p->precision;
+    info->n1 = p->g.n1;
+    info->n2 = p->g.n2;
+    info->halo = p->g.H;
+    info->rows = p->g.Ra;
+    info->cols = p->g.C;
+    info->tile = p->g.T;
+    info->tiles1 = p->g.tiles1;
+    info->tiles2 = p->g.tiles2;
+    info->patch_rows = p->g.PR;
+    info->patch_cols = p->g.PC;
+    info->chunk = p->chunk;
+    info->gather_variant = p->gather_variant;
+    info->spread_variant = p->spread_variant;
+    info->M = p->points_valid ? p->M : 0;
+    info->n_chunks = p->points_valid ? p->n_chunks : 0;
+    info->workspace_bytes = p->workspace_bytes;
+    return NFFT2D_OK;
+}
+
+static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    if (M < 0 || M > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;
+    if (coord_dtype != NFFT2D_COORD_F32 && coord_dtype != NFFT2D_COORD_F64) return NFFT2D_ERR_INVALID_ARG;
+    if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
+        return NFFT2D_ERR_INVALID_ARG;
+    if (M > 0 && (!x1 || !x2)) return NFFT2D_ERR_INVALID_ARG;
+    p->points_valid = false;
+    p->M = 0;
+    p->n_chunks = 0;
+    timer_reset(p, CALL_SORT);
+    int st = ensure_points_capacity(p, M);
+    if (st != NFFT2D_OK) return st;
+    p->workspace_bytes = plan_workspace_bytes(p);
+    if (M == 0) {
+        p->points_valid = true;
+        return NFFT2D_OK;
+    }
+    const Geom &g = p->g;
+    double u1 = 1.0, u2 = 1.0;
+    if (units == NFFT2D_UNITS_UNIT) {
+        u1 = p->N1;
+        u2 = p->N2;
+    } else if (units == NFFT2D_UNITS_RADIANS) {
+        u1 = p->N1 / (2.0 * kPi);
+        u2 = p->N2 / (2.0 * kPi);
+    }
+    const double s1 = p->sigma * u1, s2 = p->sigma * u2;
+    p->xscale1 = s1;
+    p->xscale2 = s2;
+    stage_begin(p, ST_SORT);
+    NFFT_TRY_CUDA(cudaMemsetAsync(p->d_status, 0, 4 * sizeof(int), p->stream));
+    NFFT_TRY_CUDA(cudaMemsetAsync(p->cell_count, 0, sizeof(unsigned) * (p->ncells + 1), p->stream));
+    const int Mi = static_cast<int>(M);
+    const int blocks = (Mi + 255) / 256;
+    if (p->precision == NFFT2D_F64) {
+        if (coord_dtype == NFFT2D_COORD_F64)
+            k_bin_pass1<double, Rec64><<<blocks, 256, 0, p->stream>>>(
+                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, s1, s2, g,
+                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+        else
+            k_bin_pass1<float, Rec64><<<blocks, 256, 0, p->stream>>>(
+                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, s1, s2, g,
+                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+    } else {
+        if (coord_dtype == NFFT2D_COORD_F64)
+            k_bin_pass1<double, Rec32><<<blocks, 256, 0, p->stream>>>(
+                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, s1, s2, g,
+                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+        else
+            k_bin_pass1<float, Rec32><<<blocks, 256, 0, p->stream>>>(
+                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, s1, s2, g,
+                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+    }
+    NFFT_TRY_CUDA(cudaGetLastError());
+    NFFT_TRY_CUDA(exclusive_scan(p->cell_count, p->ncells + 1, p->scan_tmp, p->stream));
+    if (p->precision == NFFT2D_F64)
+        k_bin_scatter<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->tmp_recs), p->ranks,
+                                                            p->cell_count, Mi, static_cast<Rec64 *>(p->recs));
+    else
+        k_bin_scatter<Rec32><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec32 *>(p->tmp_recs), p->ranks,
+                                                            p->cell_count, Mi, static_cast<Rec32 *>(p->recs));
+    NFFT_TRY_CUDA(cudaGetLastError());
+    const int ntiles = g.tiles1 * g.tiles2;
+    const int cpt = g.T * g.T;
+    k_tile_chunk_count<<<(ntiles + 1 + 255) / 256, 256, 0, p->stream>>>(p->cell_count, ntiles, cpt, p->chunk,
+                                                                        p->tile_chunks);
+    NFFT_TRY_CUDA(cudaGetLastError());
+    NFFT_TRY_CUDA(exclusive_scan(p->tile_chunks, ntiles + 1, p->scan_tmp, p->stream));
+    k_emit_chunks<<<(ntiles + 255) / 256, 256, 0, p->stream>>>(p->cell_count, p->tile_chunks, ntiles, cpt, p->chunk,
+                                                               p->chunks, p->d_status);
+    NFFT_TRY_CUDA(cudaGetLastError());
+    stage_end(p, ST_SORT);
+    int hs[4] = {0, 0, 0, 0};
+    NFFT_TRY_CUDA(cudaMemcpyAsync(hs, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
+    if (hs[1] & kErrNonfinite) return NFFT2D_ERR_NONFINITE;
+    if (hs[0] < 0 || hs[0] > p->chunks_cap) return NFFT2D_ERR_INTERNAL;
+    p->n_chunks = hs[0];
+    p->M = M;
+    p->points_valid = true;
+    return NFFT2D_OK;
+}
+
+static int nfft2d_type2_impl(nfft2d_plan p, int sign, const void *F, void *f) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    if (sign != 1 && sign != -1) return NFFT2D_ERR_INVALID_ARG;
+    if (!p->points_valid) return NFFT2D_ERR_NO_POINTS;
+    if (!F || (p->M > 0 && !f)) return NFFT2D_ERR_INVALID_ARG;
+    timer_reset(p, CALL_TYPE2);
+    if (p->M == 0) return NFFT2D_OK;
+    int st = type2_prepare(p, sign, F);
+    if (st != NFFT2D_OK) return st;
+    stage_begin(p, ST_GATHER);
+    NFFT_TRY_CUDA(launch_gather(p, f));
+    stage_end(p, ST_GATHER);
+    return NFFT2D_OK;
+}
+
+static int nfft2d_type1_impl(nfft2d_plan p, int sign, const void *f, void *F) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    if (sign != 1 && sign != -1) return NFFT2D_ERR_INVALID_ARG;
+    if (!p->points_valid) return NFFT2D_ERR_NO_POINTS;
+    if (!F || (p->M > 0 && !f)) return NFFT2D_ERR_INVALID_ARG;
+    timer_reset(p, CALL_TYPE1);
+    const Geom &g = p->g;
+    if (p->M == 0) {
+        NFFT_TRY_CUDA(cudaMemsetAsync(F, 0, cplx_size(p->precision) * p->N1 * p->N2, p->stream));
+        return NFFT2D_OK;
+    }
+    stage_begin(p, ST_SPREAD);
+    NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C, p->stream));
+    NFFT_TRY_CUDA(launch_spread(p, f));
+    stage_end(p, ST_SPREAD);
+    stage_begin(p, ST_FOLD);
+    NFFT_TRY_CUDA(launch_halo_fold(p));
+    stage_end(p, ST_FOLD);
+    stage_begin(p, ST_FFT1);
+    int st = run_fft(p, sign);
+    if (st != NFFT2D_OK) return st;
+    stage_end(p, ST_FFT1);
+    stage_begin(p, ST_CROP);
+    NFFT_TRY_CUDA(launch_crop(p, F));
+    stage_end(p, ST_CROP);
+    return NFFT2D_OK;
+}
+
+static int nfft2d_grad_x_impl(nfft2d_plan p, int sign, const void *F, const void *v, void *g1, void *g2);
+
+int nfft2d_set_points(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
+    const int st = nfft2d_set_points_impl(p, M, x1, x2, coord_dtype, units);
+    return st;
+}
+
+int nfft2d_type2(nfft2d_plan p, int sign, const void *F, void *f) {
+    const int st = nfft2d_type2_impl(p, sign, F, f);
+    return st;
+}
+
+int nfft2d_type1(nfft2d_plan p, int sign, const void *f, void *F) {
+    const int st = nfft2d_type1_impl(p, sign, f, F);
+    return st;
+}
+
+int nfft2d_grad_x(nfft2d_plan p, int sign, const void *F, const void *v, void *g1, void *g2) {
+    const int st = nfft2d_grad_x_impl(p, sign, F, v, g1, g2);
+    return st;
+}
+
+int nfft2d_forward(nfft2d_plan p, const void *F, void *f) { return nfft2d_type2(p, -1, F, f); }
+int nfft2d_adjoint(nfft2d_plan p, const void *f, void *F) { return nfft2d_type1(p, +1, f, F); }
+int nfft2d_spread_ref(nfft2d_plan p, const void *f, void *F) { return nfft2d_type1(p, -1, f, F); }
+
+static int nfft2d_grad_x_impl(nfft2d_plan p, int sign, const void *F, const void *v, void *g1, void *g2) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    if (sign != 1 && sign != -1) return NFFT2D_ERR_INVALID_ARG;
+    if (!p->points_valid) return NFFT2D_ERR_NO_POINTS;
+    if (!F || (p->M > 0 && (!v || !g1 || !g2))) return NFFT2D_ERR_INVALID_ARG;
+    timer_reset(p, CALL_TYPE2);
+    if (p->M == 0) return NFFT2D_OK;
+    int st = type2_prepare(p, sign, F);
+    if (st != NFFT2D_OK) return st;
+    stage_begin(p, ST_GATHER);
+    NFFT_TRY_CUDA(launch_grad(p, v, g1, g2));
+    stage_end(p, ST_GATHER);
+    return NFFT2D_OK;
+}
+
+int nfft2d_synchronize(nfft2d_plan p) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    int hs[4] = {0, 0, 0, 0};
+    NFFT_TRY_CUDA(cudaMemcpyAsync(hs, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
+    NFFT_TRY_CUDA(cudaGetLastError());
+    if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
+    if (hs[1] & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
+    return NFFT2D_OK;
+}
+
+int nfft2d_enable_timing(nfft2d_plan p, int on) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
+    p->timer.on = on != 0;
+    for (bool &u : p->timer.used) u = false;
+    return NFFT2D_OK;
+}
+
+int nfft2d_get_timings(nfft2d_plan p, nfft2d_timings *t) {
+    if (!p || !t) return NFFT2D_ERR_INVALID_ARG;
+    std::memset(t, 0, sizeof(*t));
+    if (!p->timer.on) return NFFT2D_OK;
+    NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
+    float *fields[ST_COUNT] = {&t->sort_ms,   &t->pad_ms,  &t->fft_type2_ms, &t->halo_fill_ms, &t->gather_ms,
+                               &t->spread_ms, &t->fold_ms, &t->fft_type1_ms, &t->crop_ms};
+    for (int s = 0; s < ST_COUNT; ++s) {
+        if (!p->timer.used[s]) continue;
+        float ms = 0;
+        NFFT_TRY_CUDA(cudaEventElapsedTime(&ms, p->timer.ev[2 * s], p->timer.ev[2 * s + 1]));
+        *fields[s] = ms;
+    }
+    return NFFT2D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,297 @@
+"""Host-side mirror of the reference's 2D NFFT call surface, over the C ABI.
+
+Device memory and streams come from PyTorch; every transform runs in
+libnfft2d_gb300.so (hand-written sm_103a kernels + cuFFT).  There is no
+CPU path: calls fail loudly if the library or a GPU is missing.
+
+Reference interface mirrored (same names, argument meaning and layout):
+  * ``NFFT2_2D(data, x1, x2, M1, M2)``   NFFT/NFFT2/Matlab/NFFT2_2D.m:1
+  * ``NFFT1_2D(data, x1, x2)``           BP_FBP_FFBP/NFFT1_2D.m:1
+  * ``NDFT2_2D(data, x, y, N, M)``        NFFT/NFFT2/Matlab/NDFT2_2D.m:1
+  * ``NFFT2_2D_GPU(result, data, x, y, N1, N2, M)``  NFFT/NFFT2_2D.cu:329,413
+  * ``NDFT2_2D_GPU(X, Y, u, v, d_in, d_out, Nu, Nv, M, N)``  NFFT/NDFT2_2D.cu:37
+  * ``Calculate_cuFFT_plan_C2C_NFFT2_2D`` / ``..._Z2Z_...`` /
+    ``Destroy_cuFFT_plan_NFFT2_2D``      NFFT/NFFT2_2D.cu:49-55
+Coordinates of these functions are in the reference's grid units (a point
+spans one period over [-N/2, N/2)); the window is fixed at c = 2, K = 6 as
+in the reference.  ``Plan`` exposes the general interface (any sigma, K,
+units, both signs, gradients, timing).
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+import torch
+
+from . import _lib
+from ._lib import NFFT2DError, check
+
+_REF_SIGMA = 2.0  # NFFT2_2D.cu:20 (cc), NFFT1_2D.m:9 (c)
+_REF_K = 6        # NFFT2_2D.cu:21 (K),  NFFT1_2D.m:10 (K)
+
+
+def _ptr(t: torch.Tensor | None) -> ctypes.c_void_p:
+    if t is None:
+        return ctypes.c_void_p(0)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _require_cuda(t: torch.Tensor, name: str, dtype: torch.dtype, numel: int | None = None) -> torch.Tensor:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must have dtype {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if numel is not None and t.numel() != numel:
+        raise ValueError(f"{name} must have {numel} elements, got {t.numel()}")
+    return t
+
+
+class Plan:
+    """A 2D NFFT plan: N1 x N2 coefficients, oversampling sigma, window
+    half-width K (2K+1 taps per dimension), precision 'f32' or 'f64'.
+
+    Wraps nfft2d_plan_create / set_points / forward / adjoint / spread_ref /
+    type1 / type2 / grad_x.  The plan runs on a CUDA stream (default: torch's
+    current stream at creation)."""
+
+    def __init__(self, N1: int, N2: int, sigma: float = 2.0, K: int = 6, precision: str = "f32",
+                 stream: torch.cuda.Stream | None = None):
+        self._lib = _lib.load()
+        if precision not in ("f32", "f64"):
+            raise ValueError("precision must be 'f32' or 'f64'")
+        self.N1, self.N2, self.sigma, self.K = int(N1), int(N2), float(sigma), int(K)
+        self.precision = precision
+        self.cdtype = torch.complex64 if precision == "f32" else torch.complex128
+        self.rdtype = torch.float32 if precision == "f32" else torch.float64
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        h = ctypes.c_void_p()
+        prec = _lib.F32 if precision == "f32" else _lib.F64
+        check(self._lib.nfft2d_plan_create(ctypes.byref(h), self.N1, self.N2, self.sigma, self.K, prec,
+                                           ctypes.c_void_p(self.stream.cuda_stream)), "nfft2d_plan_create")
+        self._h = h
+        self.M = 0
+        self._keep = ()
+
+    # -- life cycle -------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.nfft2d_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def set_stream(self, stream: torch.cuda.Stream) -> None:
+        self.stream = stream
+        check(self._lib.nfft2d_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "nfft2d_set_stream")
+
+    def set_tuning(self, tile: int = 0, chunk: int = 0, gather_variant: int = 0, spread_variant: int = 0,
+                   compensated: int = -1) -> None:
+        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated)
+        check(self._lib.nfft2d_set_tuning(self._h, ctypes.byref(t)), "nfft2d_set_tuning")
+
+    def info(self) -> dict:
+        i = _lib.Info()
+        check(self._lib.nfft2d_get_info(self._h, ctypes.byref(i)), "nfft2d_get_info")
+        return i.as_dict()
+
+    def enable_timing(self, on: bool = True) -> None:
+        check(self._lib.nfft2d_enable_timing(self._h, int(bool(on))), "nfft2d_enable_timing")
+
+    def timings(self) -> dict:
+        t = _lib.Timings()
+        check(self._lib.nfft2d_get_timings(self._h, ctypes.byref(t)), "nfft2d_get_timings")
+        return t.as_dict()
+
+    def synchronize(self) -> None:
+        check(self._lib.nfft2d_synchronize(self._h), "nfft2d_synchronize")
+
+    # -- points -------------------------------------------------------------
+    def set_points(self, x1: torch.Tensor, x2: torch.Tensor, units: str = "unit") -> None:
+        """Bin and sort the points.  x1 pairs with N1 (rows), x2 with N2.
+        units: 'grid' (reference: period N), 'unit' (period 1) or 'radians'."""
+        if x1.shape != x2.shape or x1.dim() != 1:
+            raise ValueError("x1 and x2 must be 1-D tensors of equal length")
+        if x1.dtype not in (torch.float32, torch.float64) or x2.dtype != x1.dtype:
+            raise TypeError("coordinates must both be float32 or both float64")
+        _require_cuda(x1, "x1", x1.dtype)
+        _require_cuda(x2, "x2", x1.dtype)
+        cd = _lib.COORD_F32 if x1.dtype == torch.float32 else _lib.COORD_F64
+        M = x1.numel()
+        check(self._lib.nfft2d_set_points(self._h, M, _ptr(x1), _ptr(x2), cd, _lib.UNITS[units]),
+              "nfft2d_set_points")
+        self.M = M
+        self._keep = (x1, x2)
+
+    # -- transforms ---------------------------------------------------------
+    def _coef(self, F: torch.Tensor, name: str = "F") -> torch.Tensor:
+        F = _require_cuda(F, name, self.cdtype, self.N1 * self.N2)
+        return F
+
+    def _vals(self, f: torch.Tensor, name: str = "f") -> torch.Tensor:
+        return _require_cuda(f, name, self.cdtype, self.M)
+
+    def type2(self, sign: int, F: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """f_p = sum_k F_k exp(sign 2 pi i k.x_p / N)."""
+        F = self._coef(F)
+        out = torch.empty(self.M, dtype=self.cdtype, device=F.device) if out is None else self._vals(out, "out")
+        check(self._lib.nfft2d_type2(self._h, int(sign), _ptr(F), _ptr(out)), "nfft2d_type2")
+        return out
+
+    def type1(self, sign: int, f: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """F_k = sum_p f_p exp(sign 2 pi i k.x_p / N), returned N1 x N2."""
+        f = self._vals(f)
+        out = (torch.empty(self.N1, self.N2, dtype=self.cdtype, device=f.device) if out is None
+               else self._coef(out, "out"))
+        check(self._lib.nfft2d_type1(self._h, int(sign), _ptr(f), _ptr(out)), "nfft2d_type1")
+        return out
+
+    def forward(self, F: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Type 2 with the reference's sign (NFFT1_2D)."""
+        return self.type2(-1, F, out)
+
+    def adjoint(self, f: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Hermitian adjoint of forward: type 1 with sign +1."""
+        return self.type1(+1, f, out)
+
+    def spread_ref(self, f: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Type 1 with the reference's sign (NFFT2_2D)."""
+        return self.type1(-1, f, out)
+
+    def grad_x(self, F: torch.Tensor, v: torch.Tensor, sign: int = -1):
+        """(Re(conj(v) df/dx1), Re(conj(v) df/dx2)) for f = type2(sign, F),
+        in the units given to set_points."""
+        F = self._coef(F)
+        v = self._vals(v, "v")
+        g1 = torch.empty(self.M, dtype=self.rdtype, device=F.device)
+        g2 = torch.empty_like(g1)
+        check(self._lib.nfft2d_grad_x(self._h, int(sign), _ptr(F), _ptr(v), _ptr(g1), _ptr(g2)),
+              "nfft2d_grad_x")
+        return g1, g2
+
+
+# ---------------------------------------------------------------------------
+# Reference call surface (c = 2, K = 6, grid-unit coordinates)
+# ---------------------------------------------------------------------------
+_cache_lock = threading.Lock()
+_plan_cache: dict[tuple, Plan] = {}
+
+
+def _cached_plan(N1: int, N2: int, precision: str) -> Plan:
+    key = (int(N1), int(N2), precision, torch.cuda.current_device())
+    with _cache_lock:
+        p = _plan_cache.get(key)
+        if p is None:
+            p = Plan(N1, N2, _REF_SIGMA, _REF_K, precision)
+            _plan_cache[key] = p
+        return p
+
+
+def _prec_of(t: torch.Tensor) -> str:
+    if t.dtype in (torch.complex64, torch.float32):
+        return "f32"
+    if t.dtype in (torch.complex128, torch.float64):
+        return "f64"
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def Calculate_cuFFT_plan_C2C_NFFT2_2D(N1: int, N2: int) -> None:
+    """NFFT2_2D.cu:49: create the single-precision plan for N1 x N2 outputs."""
+    _cached_plan(N1, N2, "f32")
+
+
+def Calculate_cuFFT_plan_Z2Z_NFFT2_2D(N1: int, N2: int) -> None:
+    """NFFT2_2D.cu:50: create the double-precision plan for N1 x N2 outputs."""
+    _cached_plan(N1, N2, "f64")
+
+
+def Destroy_cuFFT_plan_NFFT2_2D() -> None:
+    """NFFT2_2D.cu:55: release every cached plan."""
+    with _cache_lock:
+        for p in _plan_cache.values():
+            p.close()
+        _plan_cache.clear()
+
+
+def NFFT2_2D_GPU(result: torch.Tensor, data: torch.Tensor, x: torch.Tensor, y: torch.Tensor,
+                 N1: int, N2: int, M: int) -> None:
+    """NFFT2_2D.cu:329/413: result[i, j] = sum_p data[p] exp(-2 pi i ((i-N1/2) x_p/N1 + (j-N2/2) y_p/N2)),
+    x, y in grid units; result is N1*N2 complex (row-major), written in place."""
+    prec = _prec_of(data)
+    p = _cached_plan(N1, N2, prec)
+    if x.numel() < M or y.numel() < M or data.numel() < M:
+        raise ValueError("x, y and data must hold at least M entries")
+    p.set_points(x[:M], y[:M], units="grid")
+    p.spread_ref(data[:M], out=result.view(-1) if result.dim() != 1 else result)
+    p.synchronize()
+
+
+def NDFT2_2D_GPU(X: torch.Tensor, Y: torch.Tensor, u: torch.Tensor, v: torch.Tensor, d_in: torch.Tensor,
+                 d_out: torch.Tensor, Nu: int, Nv: int, M: int, N: int, sign: int = -1) -> None:
+    """NDFT2_2D.cu:37-72: d_out[q] = sum_p d_in[p] exp(-2 pi i (u_q X_p/Nu + v_q Y_p/Nv)), FP64,
+    matrix-free (no cuBLAS handle, no file dump)."""
+    for t, n in ((X, "X"), (Y, "Y"), (u, "u"), (v, "v")):
+        _require_cuda(t, n, torch.float64)
+    _require_cuda(d_in, "d_in", torch.complex128)
+    _require_cuda(d_out, "d_out", torch.complex128)
+    lib = _lib.load()
+    check(lib.nfft2d_ndft2d_f64(_ptr(X), _ptr(Y), _ptr(u), _ptr(v), _ptr(d_in), _ptr(d_out), int(Nu), int(Nv),
+                                int(M), int(N), int(sign), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+          "nfft2d_ndft2d_f64")
+
+
+def NFFT2_2D(data: torch.Tensor, x1: torch.Tensor, x2: torch.Tensor, M1: int, M2: int) -> torch.Tensor:
+    """NFFT2_2D.m:1: transf(k1, k2) = sum_p data_p exp(-2 pi i (k1 x1_p / M1 + k2 x2_p / M2)),
+    k in [-M/2, M/2), returned M1 x M2 (row <-> x1)."""
+    p = _cached_plan(M1, M2, _prec_of(data))
+    p.set_points(x1.contiguous(), x2.contiguous(), units="grid")
+    return p.spread_ref(data.contiguous().view(-1))
+
+
+def NFFT1_2D(data: torch.Tensor, x1: torch.Tensor, x2: torch.Tensor) -> torch.Tensor:
+    """BP_FBP_FFBP/NFFT1_2D.m:1: result_p = sum_k data(k1, k2) exp(-2 pi i (k1 x1_p / N1 + k2 x2_p / N2)),
+    data N1 x N2 with row <-> k1 = i - N1/2."""
+    N1, N2 = data.shape
+    p = _cached_plan(N1, N2, _prec_of(data))
+    p.set_points(x1.contiguous(), x2.contiguous(), units="grid")
+    return p.forward(data.contiguous())
+
+
+def NDFT2_2D(data: torch.Tensor, x: torch.Tensor, y: torch.Tensor, N: int, M: int) -> torch.Tensor:
+    """NDFT2_2D.m:1 layout: returns N x M with element (r, s) pairing the
+    y-frequency v = r - M/2 ... as in the MATLAB reshape: (r, s) holds
+    sum_p data_p exp(-2 pi i (x_p u_s / N + y_p v_r / M)), u_s = s - N/2,
+    v_r = r - M/2, for N == M (the MATLAB divides the y-term by N, which is
+    the same thing when N == M; for N != M the intended /M is used).  Exact
+    FP64 direct sum on the GPU."""
+    if N != M:
+        raise NFFT2DError(_lib.ERR_UNSUPPORTED, "NDFT2_2D: the reference layout is defined for N == M")
+    dev = data.device
+    u = torch.arange(N, device=dev, dtype=torch.float64) - N // 2
+    v = torch.arange(M, device=dev, dtype=torch.float64) - M // 2
+    # output (r, s) row-major: q = r * M + s; r <-> v, s <-> u
+    vv, uu = torch.meshgrid(v, u, indexing="ij")
+    out = torch.empty(N * M, dtype=torch.complex128, device=dev)
+    NDFT2_2D_GPU(x.to(torch.float64).contiguous(), y.to(torch.float64).contiguous(), uu.reshape(-1).contiguous(),
+                 vv.reshape(-1).contiguous(), data.to(torch.complex128).contiguous(), out, N, M, x.numel(), N * M)
+    return out.view(N, M)
+
+
+__all__ = ["Plan", "NFFT2DError", "NFFT2_2D", "NFFT1_2D", "NDFT2_2D", "NFFT2_2D_GPU", "NDFT2_2D_GPU",
+           "Calculate_cuFFT_plan_C2C_NFFT2_2D", "Calculate_cuFFT_plan_Z2Z_NFFT2_2D", "Destroy_cuFFT_plan_NFFT2_2D"]

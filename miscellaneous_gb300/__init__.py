@@ -12,7 +12,7 @@ __all__ = ["NFFT2DError", "LIB_PATH", "load", "nfft"]
 
 def __getattr__(name):
     # torch is imported lazily so the C-ABI checks run without it.
-    if name == "nfft":
-        from . import nfft
-        return nfft
+    if name in ("nfft", "shard"):
+        import importlib
+        return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)

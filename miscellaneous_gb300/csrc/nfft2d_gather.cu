@@ -41,7 +41,7 @@ __device__ __forceinline__ void issue_patch(const CUtensorMap *map, const int4 *
 
 // MODE 0: f = gather(grid);  MODE 1: coordinate gradient contracted with vin.
 template <int K, bool COMP, int MODE>
-__global__ void __launch_bounds__(kThreads) k_gather_tiled(const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(const __grid_constant__ CUtensorMap tmap,
                                                            const Rec32 *__restrict__ recs,
                                                            const int4 *__restrict__ chunks, float2 *__restrict__ out,
                                                            const float2 *__restrict__ vin, float *__restrict__ g1,

@@ -55,6 +55,7 @@ extern "C" {
 #define NFFT2D_ERR_DEVICE_BOUNDS   -8  /* a kernel rejected an out-of-tile record */
 #define NFFT2D_ERR_UNSUPPORTED     -9  /* valid request this build does not serve */
 #define NFFT2D_ERR_INTERNAL       -10
+#define NFFT2D_ERR_SCRATCH_LIMIT  -11  /* size beyond the fixed scratch of the no-allocation entry point */
 
 /* ---- enums ------------------------------------------------------------ */
 #define NFFT2D_F32 0   /* complex64 data, FP32 kernels (FP64 plan-time math) */
@@ -178,6 +179,30 @@ int nfft2d_device_count(void);
 int nfft2d_ndft2d_f64(const double *X, const double *Y, const double *u, const double *v,
                       const void *in, void *out, int Nu, int Nv, long long M, long long N,
                       int sign, void *stream);
+
+/* ---- forward transform that allocates nothing ----------------------------
+ * No counterpart in the reference: an addition for callers that must not
+ * allocate device memory while they run -- a host application that owns all
+ * device memory through its own pool (a MATLAB MEX gateway working on
+ * gpuArray data, for instance), a latency-critical loop that cannot afford
+ * cudaMalloc's implicit synchronisation, or code launched inside a CUDA-graph
+ * stream capture, where cudaMalloc is not permitted.
+ *
+ * Same result as nfft2d_forward on a plan (N1, N2, sigma = 2, K), computed
+ * without a plan: f_p = sum_k F_k exp(-2 pi i (k1 x1_p / N1 + k2 x2_p / N2)).
+ * x1, x2: M FP32 coordinates in `units`; F: N1 x N2 complex64; f: M complex64;
+ * all device pointers owned by the caller; runs asynchronously on `stream`.
+ *
+ * Limits: N1, N2 even and <= 128, 2 <= K <= 8; larger grids return
+ * NFFT2D_ERR_SCRATCH_LIMIT.  Every work buffer lives in one fixed 1.12 MB
+ * device array inside the library (held on each GPU that loads it until the
+ * process exits); no cudaMalloc, cudaFree or allocating library call is made.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture begins.  All
+ * calls share the array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller. */
+int nfft2d_forward_small_noalloc(int N1, int N2, int K, long long M, const float *x1, const float *x2, int units,
+                                 const void *F, void *f, void *stream);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,7 @@ ERR_DEVICE_TIMEOUT = -7
 ERR_DEVICE_BOUNDS = -8
 ERR_UNSUPPORTED = -9
 ERR_INTERNAL = -10
+ERR_SCRATCH_LIMIT = -11
 
 F32 = 0
 F64 = 1
@@ -98,6 +99,7 @@ _SIGNATURES = {
     "nfft2d_status_string": (ctypes.c_char_p, [_I]),
     "nfft2d_device_count": (_I, []),
     "nfft2d_ndft2d_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _LL, _LL, _I, _P]),
+    "nfft2d_forward_small_noalloc": (_I, [_I, _I, _I, _LL, _P, _P, _I, _P, _P, _P]),
 }
 
 

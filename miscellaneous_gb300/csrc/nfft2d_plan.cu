@@ -715,6 +715,7 @@ const char *nfft2d_status_string(int s) {
         case NFFT2D_ERR_DEVICE_BOUNDS: return "device-side bounds check failed";
         case NFFT2D_ERR_UNSUPPORTED: return "unsupported request";
         case NFFT2D_ERR_INTERNAL: return "internal error";
+        case NFFT2D_ERR_SCRATCH_LIMIT: return "size exceeds the fixed scratch of the no-allocation entry point";
         default: return "unknown status";
     }
 }

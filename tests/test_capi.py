@@ -58,7 +58,7 @@ void f(float2* r, const float2* d, const float* x, const float* y,
 
 
 def test_status_strings(lib):
-    for code in range(0, -11, -1):
+    for code in range(0, -12, -1):
         s = _lib.status_string(code)
         assert s and s != "unknown status"
     assert _lib.status_string(-999) == "unknown status"

@@ -14,6 +14,7 @@ struct KArgs {
     double ds1_d, ds2_d;
     int n_chunks;            // work items (tiled kernels)
     int M;                   // points (direct kernels)
+    int chunk;               // maximum points per work item of the chunk list
     int *status;             // [1]: latched error bits
 };
 
@@ -31,6 +32,7 @@ inline KArgs make_kargs(const nfft2d_plan_s *p) {
     a.ds2_d = p->xscale2;
     a.n_chunks = static_cast<int>(p->n_chunks);
     a.M = static_cast<int>(p->M);
+    a.chunk = p->chunk;
     a.status = p->d_status;
     return a;
 }

@@ -39,8 +39,17 @@ constexpr int kThreads = 256;
 
 constexpr int kSpreadWarps = 4;  // warps per CTA of the tiled spread
 constexpr int kRegTile = 16;     // tile edge the register-resident spread requires
-// Per-point scratch (floats): lr, lc, v.x, v.y, w1[16] (2K+1 used), w2[16].
-constexpr int kPointScratch = 36;
+constexpr int kSpreadItem = 128; // points per warp work item (a chunk is split into items)
+// Per-point scratch (floats): lr, lc, v.x, v.y, then w1 and w2, each padded
+// to a multiple of 4 floats (2K+1 used).
+template <int K>
+constexpr int wpad() {
+    return ((2 * K + 1 + 3) / 4) * 4;
+}
+template <int K>
+constexpr int point_scratch() {
+    return 4 + 2 * wpad<K>();
+}
 
 // cp.async.bulk.wait_group.read 0: the warp's last reduction has finished
 // reading its shared-memory source.
@@ -49,7 +58,7 @@ __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bu
 // acc[L + a] += (ax, ay) * w1[a] for the 2K+1 rows of a point whose first
 // patch row is L (compile-time, so acc stays in registers).
 template <int K, int PR, int L>
-__device__ __forceinline__ void add_rows(float2 (&acc)[PR], const float (&w1)[16], float ax, float ay) {
+__device__ __forceinline__ void add_rows(float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax, float ay) {
 #pragma unroll
     for (int a = 0; a <= 2 * K; ++a) {
         acc[L + a].x = fmaf(ax, w1[a], acc[L + a].x);
@@ -57,14 +66,24 @@ __device__ __forceinline__ void add_rows(float2 (&acc)[PR], const float (&w1)[16
     }
 }
 
-template <int K, int PR, int L>
-__device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const float (&w1)[16], float ax, float ay) {
-    if constexpr (L < kRegTile) {
-        if (lr == L)
-            add_rows<K, PR, L>(acc, w1, ax, ay);
-        else
-            add_rows_switch<K, PR, L + 1>(lr, acc, w1, ax, ay);
+// Dispatch on the point's first patch row with a jump table (the row offset
+// is warp-uniform, so every lane takes the same case).
+template <int K, int PR>
+__device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax,
+                                                float ay) {
+    static_assert(kRegTile == 16, "one case per row of a 16-row tile");
+#define NFFT2D_ROW_CASE(L)                          \
+    case L:                                         \
+        add_rows<K, PR, L>(acc, w1, ax, ay);        \
+        break;
+    switch (lr) {
+        NFFT2D_ROW_CASE(0) NFFT2D_ROW_CASE(1) NFFT2D_ROW_CASE(2) NFFT2D_ROW_CASE(3)
+        NFFT2D_ROW_CASE(4) NFFT2D_ROW_CASE(5) NFFT2D_ROW_CASE(6) NFFT2D_ROW_CASE(7)
+        NFFT2D_ROW_CASE(8) NFFT2D_ROW_CASE(9) NFFT2D_ROW_CASE(10) NFFT2D_ROW_CASE(11)
+        NFFT2D_ROW_CASE(12) NFFT2D_ROW_CASE(13) NFFT2D_ROW_CASE(14) NFFT2D_ROW_CASE(15)
+        default: break;
     }
+#undef NFFT2D_ROW_CASE
 }
 
 template <int K>
@@ -82,17 +101,24 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pstride = patch_stride_elems(g);
     float2 *patch = bufs + warp * pstride;  // this warp's flush buffer, PR x 32
-    float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * kPointScratch;
+    constexpr int SP = point_scratch<K>(), WP = wpad<K>();
+    float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * SP;
     const int n = a.n_chunks;
     int *work = a.status + 2;  // work-item counter, zeroed before the launch
     bool pending = false;
 
+    const int parts = (a.chunk + kSpreadItem - 1) / kSpreadItem;  // items per chunk
     for (;;) {
-        int c = 0;
-        if (lane == 0) c = atomicAdd(work, 1);
-        c = __shfl_sync(0xffffffffu, c, 0);
-        if (c >= n) break;
-        const int4 ch = __ldg(&chunks[c]);
+        int item = 0;
+        if (lane == 0) item = atomicAdd(work, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= n * parts) break;
+        const int c = item / parts, part = item - c * parts;
+        int4 ch = __ldg(&chunks[c]);
+        const int first = part * kSpreadItem;
+        if (first >= ch.z) continue;  // this chunk has fewer points
+        ch.y += first;
+        ch.z = min(kSpreadItem, ch.z - first);
         const int tr = ch.x / g.tiles2, tc = ch.x - tr * g.tiles2;
         const int r0 = tr * kRegTile, c0 = tc * kRegTile;
 
@@ -117,22 +143,22 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
                 float w1[W], w2[W];
                 weights_f32<K>(__int_as_float(raw.x), w1, a.alpha, a.cn, a.kp);
                 weights_f32<K>(__int_as_float(raw.y), w2, a.alpha, a.cn, a.kp);
-                float *sp = scr + lane * kPointScratch;
+                float *sp = scr + lane * SP;
                 reinterpret_cast<float4 *>(sp)[0] = make_float4(__int_as_float(lr), __int_as_float(lc), v.x, v.y);
 #pragma unroll
-                for (int k = 0; k < 16; ++k) sp[4 + k] = k < W ? w1[k] : 0.f;
+                for (int k = 0; k < WP; ++k) sp[4 + k] = k < W ? w1[k] : 0.f;
 #pragma unroll
-                for (int k = 0; k < 16; ++k) sp[20 + k] = k < W ? w2[k] : 0.f;
+                for (int k = 0; k < WP; ++k) sp[4 + WP + k] = k < W ? w2[k] : 0.f;
             }
             __syncwarp();
             // 2) the warp walks the points; lane = patch column
             for (int j = 0; j < nb; ++j) {
-                const float *sp = scr + j * kPointScratch;
+                const float *sp = scr + j * SP;
                 const float4 meta = reinterpret_cast<const float4 *>(sp)[0];
                 const int lr = __float_as_int(meta.x), lc = __float_as_int(meta.y);
-                float w1[16];
+                float w1[WP];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < WP / 4; ++q) {
                     const float4 t = reinterpret_cast<const float4 *>(sp + 4)[q];
                     w1[4 * q] = t.x;
                     w1[4 * q + 1] = t.y;
@@ -140,8 +166,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
                     w1[4 * q + 3] = t.w;
                 }
                 const int b = lane - lc - (KE - K);  // this lane's tap column
-                const float w2 = (static_cast<unsigned>(b) < static_cast<unsigned>(W)) ? sp[20 + b] : 0.f;
-                add_rows_switch<K, PR, 0>(lr, acc, w1, meta.z * w2, meta.w * w2);
+                const float w2 = (static_cast<unsigned>(b) < static_cast<unsigned>(W)) ? sp[4 + WP + b] : 0.f;
+                add_rows_switch<K, PR>(lr, acc, w1, meta.z * w2, meta.w * w2);
             }
             __syncwarp();  // scratch is rewritten by the next batch
         }
@@ -203,7 +229,7 @@ cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
         p->g.PC == 32) {
         if (p->n_chunks == 0) return cudaSuccess;
         const int smem = kSpreadWarps * patch_stride_elems(p->g) * static_cast<int>(sizeof(float2)) + 128 +
-                         kSpreadWarps * 32 * kPointScratch * static_cast<int>(sizeof(float));
+                         kSpreadWarps * 32 * point_scratch<K>() * static_cast<int>(sizeof(float));
         auto kernel = k_spread_tiled<K>;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -212,7 +238,8 @@ cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
         cudaError_t e = cudaMemsetAsync(p->d_status + 2, 0, sizeof(int), p->stream);
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kSpreadWarps * 32, smem);
-        const int need = static_cast<int>((p->n_chunks + kSpreadWarps - 1) / kSpreadWarps);
+        const long long items = p->n_chunks * ((p->chunk + kSpreadItem - 1) / kSpreadItem);
+        const int need = static_cast<int>((items + kSpreadWarps - 1) / kSpreadWarps);
         if (blocks > need) blocks = need;
         kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(p->tmap, static_cast<const Rec32 *>(p->recs),
                                                                 p->chunks, static_cast<const float2 *>(f), a);

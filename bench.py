@@ -89,7 +89,23 @@ def clustered_config3(seed: int = 2, K: int = 6, M: int = 1 << 24, N: int = 2048
                         "seed": seed})
 
 
-WORKLOADS = {"polar": polar_raster, "config1": uniform_config1, "clustered": clustered_config3}
+def uneven_batch(seed: int = 3, count: int = 64):
+    """64 transforms, N = 2^e with e ~ U{7..10} (square), M log-uniform in
+    [1e4, 4e6], points uniform, coefficients N(0,1) complex; sigma 2, w 6."""
+    rng = np.random.default_rng(seed)
+    es = rng.integers(7, 11, count)
+    Ms = np.floor(10 ** rng.uniform(4, np.log10(4e6), count)).astype(np.int64)
+    items = []
+    for e, m in zip(es, Ms):
+        N = 1 << int(e)
+        items.append(dict(N=N, M=int(m)))
+    return dict(name="uneven_batch_64", items=items, seed=seed, sigma=2.0, K=6,
+                config={"workload": "uneven batch of 64 transforms", "count": count, "N": "2^U{7..10} square",
+                        "points": int(Ms.sum()), "points_per_transform": "floor(10^U(4, log10 4e6))", "sigma": 2.0,
+                        "w": 6, "seed": seed})
+
+
+WORKLOADS = {"polar": polar_raster, "config1": uniform_config1, "clustered": clustered_config3, "batch": uneven_batch}
 
 
 # ---------------------------------------------------------------------------
@@ -324,6 +340,10 @@ def run_ours(args, wl):
 
     plan = Plan(N1, N2, sigma=wl["sigma"], K=wl["K"], precision="f32", stream=stream)
     plan.set_points(x1, x2, units="unit")
+    tuned = None
+    if not args.no_autotune:
+        from miscellaneous_gb300 import autotune
+        tuned = autotune.tune(plan, x1, x2, F, f, use_cache=False)  # measured here, outside the timed region
     f_out = torch.empty(M, dtype=torch.complex64, device=dev)
     F_out = torch.empty(N1 * N2, dtype=torch.complex64, device=dev)
 
@@ -380,7 +400,9 @@ def run_ours(args, wl):
     dom = "gather" if stage["gather"] >= stage["spread"] else "spread"
     dom_ms = stage[dom]
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
-    kname = {"gather": "k_gather_tiled", "spread": "k_spread_tiled"}[dom]
+    ginfo = plan.info()
+    kname = {"gather": "k_gather_tiled" if ginfo["gather_variant"] == 1 else "k_gather_direct",
+             "spread": "k_spread_tiled" if ginfo["spread_variant"] == 1 else "k_spread_direct"}[dom]
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": dom_ms,
@@ -464,7 +486,8 @@ def run_ours(args, wl):
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(wl["config"], l2="256 MB buffer written between timed steps (working set < L2)",
-                           points_prebinned=True, parallelism="replicas" if world > 1 else "single GPU"),
+                           points_prebinned=True, parallelism="replicas" if world > 1 else "single GPU",
+                           tuning=(tuned or {}).get("tuning"), plan=plan.info()),
             "stages_ms": stage,
             "forward_ms": stage["pad"] + stage["fft_fwd"] + stage["halo_fill"] + stage["gather"],
             "adjoint_ms": stage["spread"] + stage["fold"] + stage["fft_adj"] + stage["crop"],
@@ -481,6 +504,77 @@ def run_ours(args, wl):
         dist.destroy_process_group()
 
 
+def run_batch(args, wl):
+    """Config 4: the batched graph launch vs one transform per launch (the
+    library's own single-transform path with pre-created plans)."""
+    import torch
+
+    from miscellaneous_gb300.nfft import Batch, Plan
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    g = torch.Generator(device=dev).manual_seed(wl["seed"])
+    sizes = [(it["N"], it["N"]) for it in wl["items"]]
+    x1s = [torch.rand(it["M"], device=dev, generator=g) - 0.5 for it in wl["items"]]
+    x2s = [torch.rand(it["M"], device=dev, generator=g) - 0.5 for it in wl["items"]]
+    Fs = [torch.randn(n1 * n2, dtype=torch.complex64, device=dev, generator=g) for n1, n2 in sizes]
+    fs = [torch.randn(it["M"], dtype=torch.complex64, device=dev, generator=g) for it in wl["items"]]
+    f_out = [torch.empty(it["M"], dtype=torch.complex64, device=dev) for it in wl["items"]]
+    F_out = [torch.empty(n1 * n2, dtype=torch.complex64, device=dev) for n1, n2 in sizes]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    total = sum(it["M"] for it in wl["items"])
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(step):
+        for _ in range(args.warmup):
+            step()
+            flush.zero_()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            ev0.record(stream)
+            step()
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+            flush.zero_()
+        return sum(ms) / len(ms)
+
+    batch = Batch(sizes, sigma=wl["sigma"], K=wl["K"], stream=stream)
+    batch.set_points(x1s, x2s)
+
+    def batched():
+        batch.forward(Fs, f_out)
+        batch.adjoint(fs, F_out)
+
+    t_batch = timed(batched)
+    plans = []
+    for (n1, n2), a, b in zip(sizes, x1s, x2s):
+        p = Plan(n1, n2, sigma=wl["sigma"], K=wl["K"], stream=stream)
+        p.set_points(a, b)
+        plans.append(p)
+
+    def sequential():
+        for p, F, fo in zip(plans, Fs, f_out):
+            p.forward(F, out=fo)
+        for p, f, Fo in zip(plans, fs, F_out):
+            p.adjoint(f, out=Fo)
+
+    t_seq = timed(sequential)
+    batch.synchronize()
+    line = {"metric": METRIC, "value": total / (t_batch * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_batch, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(wl["config"], l2="256 MB buffer written between timed steps"),
+            "sequential_ms_per_step": t_seq, "batched_speedup": t_seq / t_batch,
+            "sequential": "one forward + one adjoint per transform through pre-created single-transform plans",
+            "batched": "nfft2d_batch_forward + nfft2d_batch_adjoint, stage sequence replayed as a CUDA graph"}
+    print(json.dumps(line))
+    for p in plans:
+        p.close()
+    batch.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,11 +585,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]()
-    if args.impl == "reference":
+    if args.workload == "batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no reference counterpart"}))
+            return
+        run_batch(args, wl)
+    elif args.impl == "reference":
         run_reference(args, wl)
     else:
         run_ours(args, wl)

@@ -180,6 +180,29 @@ int nfft2d_ndft2d_f64(const double *X, const double *Y, const double *u, const d
                       const void *in, void *out, int Nu, int Nv, long long M, long long N,
                       int sign, void *stream);
 
+/* ---- batches: many transforms of uneven size in one go ------------------
+ * No reference counterpart: the reference runs one NFFT2_2D_GPU per PSO
+ * particle in a host loop (Synthesis/PSO/PSO.cu:348, Synthesis.cu:395).
+ * A batch holds `count` FP32 transforms (N1[t] x N2[t], shared sigma and K,
+ * 16 x 16 tiles).  Grids of equal size share one batched cuFFT plan; every
+ * other stage covers all transforms with one launch (persistent gather and
+ * spread kernels over the work items of all transforms); the stage sequence
+ * is captured into a CUDA graph on first use and replayed (set_graph(0) runs
+ * it eagerly instead).  set_points binds per-transform point arrays (FP32 or
+ * FP64 coordinates, as nfft2d_set_points) and synchronizes; forward/adjoint
+ * take host arrays of `count` device pointers and are asynchronous with
+ * respect to the host, ordered after prior work on `stream`. */
+typedef struct nfft2d_batch_s *nfft2d_batch;
+int nfft2d_batch_create(nfft2d_batch *batch, int count, const int *N1, const int *N2, double sigma, int K,
+                        void *stream);
+int nfft2d_batch_destroy(nfft2d_batch batch);
+int nfft2d_batch_set_points(nfft2d_batch batch, const long long *M, const void *const *x1, const void *const *x2,
+                            int coord_dtype, int units);
+int nfft2d_batch_forward(nfft2d_batch batch, const void *const *F, void *const *f);
+int nfft2d_batch_adjoint(nfft2d_batch batch, const void *const *f, void *const *F);
+int nfft2d_batch_set_graph(nfft2d_batch batch, int on);
+int nfft2d_batch_synchronize(nfft2d_batch batch);
+
 /* ---- forward transform that allocates nothing ----------------------------
  * No counterpart in the reference: an addition for callers that must not
  * allocate device memory while they run -- a host application that owns all

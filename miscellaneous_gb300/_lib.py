@@ -100,6 +100,13 @@ _SIGNATURES = {
     "nfft2d_device_count": (_I, []),
     "nfft2d_ndft2d_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _LL, _LL, _I, _P]),
     "nfft2d_forward_small_noalloc": (_I, [_I, _I, _I, _LL, _P, _P, _I, _P, _P, _P]),
+    "nfft2d_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _P, _D, _I, _P]),
+    "nfft2d_batch_destroy": (_I, [_P]),
+    "nfft2d_batch_set_points": (_I, [_P, _P, _P, _P, _I, _I]),
+    "nfft2d_batch_forward": (_I, [_P, _P, _P]),
+    "nfft2d_batch_adjoint": (_I, [_P, _P, _P]),
+    "nfft2d_batch_set_graph": (_I, [_P, _I]),
+    "nfft2d_batch_synchronize": (_I, [_P]),
 }
 
 

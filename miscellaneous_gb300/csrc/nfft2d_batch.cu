@@ -1,0 +1,652 @@
+// nfft2d_batch.cu -- many independent 2D NFFTs of uneven size in one go.
+//
+// Layout: one plan per transform (its own binning, records and work list),
+// but every padded grid lives in ONE allocation, grouped by size, so the
+// FFTs of a size group run as one batched cuFFT call.  Each stage then covers
+// all transforms with a single launch: deapodize + pad, halo fill / fold and
+// crop walk (transform, row) pairs; the gather is a persistent kernel over
+// the concatenated work items of all transforms (TMA-staged patches); the
+// spread is a persistent warp kernel over the same items (register-resident
+// patches, one TMA reduce-add per item).  Per-transform descriptors -- the
+// TMA tensor map, geometry, record and work-item pointers -- sit in device
+// memory; the per-call input/output pointers go to a small device table
+// copied before each run.  The stage sequence is captured once into a CUDA
+// graph and replayed, so a batch costs one graph launch plus that copy.
+//
+// No reference counterpart: the reference runs one NFFT2_2D_GPU per PSO
+// particle in a host loop (Synthesis/PSO/PSO.cu:348, Synthesis.cu:395).
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "nfft2d_device.cuh"
+#include "nfft2d_internal.h"
+#include "nfft2d_kargs.cuh"
+#include "nfft2d_tile_ops.cuh"
+
+using namespace nfft2d;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kSpreadWarps = 4;
+constexpr int kSpreadItem = 128;
+
+// One transform of a batch, device resident (the tensor map needs 64-byte
+// alignment; the struct keeps it first and the array is allocated aligned).
+struct alignas(128) BatchDesc {
+    CUtensorMap tmap;
+    const Rec32 *recs;
+    const int4 *chunks;
+    float2 *grid;
+    const float *deap1, *deap2;
+    Geom g;
+    int N1, N2;
+    int n_chunks;
+    int chunk_base;     // first global work item of this transform
+    int row_base;       // first global oversampled row (pad / halo kernels)
+    int crop_base;      // first global output row (crop)
+    int chunk;          // maximum points per work item
+    int pad_;
+};
+
+struct BatchIO {
+    const float2 *in;  // type 2: F (N1*N2); type 1: f (M)
+    float2 *out;       // type 2: f (M);     type 1: F (N1*N2)
+};
+
+// Index of the transform whose [base, next base) holds key (bases ascending).
+template <int FIELD>
+__device__ __forceinline__ int find_transform(const BatchDesc *__restrict__ d, int n, int key) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int b = FIELD == 0 ? __ldg(&d[mid].chunk_base) : FIELD == 1 ? __ldg(&d[mid].row_base)
+                                                                           : __ldg(&d[mid].crop_base);
+        if (b <= key)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---- per-row stages over all transforms ------------------------------------
+__global__ void k_batch_pad(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io) {
+    const int t = find_transform<1>(d, n, blockIdx.x);
+    const BatchDesc &D = d[t];
+    const int r = blockIdx.x - D.row_base;
+    const int n1 = D.g.n1, n2 = D.g.n2, N1 = D.N1, N2 = D.N2;
+    const int k1 = (r < n1 / 2) ? r : r - n1;
+    const bool row_in = k1 >= -N1 / 2 && k1 < N1 / 2;
+    const int i = k1 + N1 / 2;
+    const float s1 = row_in ? D.deap1[i] : 0.f;
+    const float2 *F = io[t].in;
+    float2 *dst = D.grid + static_cast<size_t>(r + D.g.H) * D.g.C + D.g.H;
+    for (int c = threadIdx.x; c < n2; c += blockDim.x) {
+        const int k2 = (c < n2 / 2) ? c : c - n2;
+        float2 v = make_float2(0.f, 0.f);
+        if (row_in && k2 >= -N2 / 2 && k2 < N2 / 2) {
+            const int j = k2 + N2 / 2;
+            const float s = s1 * D.deap2[j];
+            const float2 f = F[static_cast<size_t>(i) * N2 + j];
+            v = make_float2(f.x * s, f.y * s);
+        }
+        dst[c] = v;
+    }
+}
+
+__global__ void k_batch_crop(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io) {
+    const int t = find_transform<2>(d, n, blockIdx.x);
+    const BatchDesc &D = d[t];
+    const int i = blockIdx.x - D.crop_base;
+    const int N1 = D.N1, N2 = D.N2, n1 = D.g.n1, n2 = D.g.n2;
+    const int k1 = i - N1 / 2;
+    const int r = k1 < 0 ? k1 + n1 : k1;
+    const float s1 = D.deap1[i];
+    const float2 *src = D.grid + static_cast<size_t>(r + D.g.H) * D.g.C + D.g.H;
+    float2 *F = io[t].out;
+    for (int j = threadIdx.x; j < N2; j += blockDim.x) {
+        const int k2 = j - N2 / 2;
+        const int c = k2 < 0 ? k2 + n2 : k2;
+        const float s = s1 * D.deap2[j];
+        const float2 g = src[c];
+        F[static_cast<size_t>(i) * N2 + j] = make_float2(g.x * s, g.y * s);
+    }
+}
+
+__device__ __forceinline__ int pmod(int a, int n) {
+    int r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+// Periodic halo fill (type 2) of transform blockIdx.y.
+__global__ void k_batch_fill(const BatchDesc *__restrict__ d) {
+    const BatchDesc &D = d[blockIdx.y];
+    const int n1 = D.g.n1, n2 = D.g.n2, H = D.g.H, C = D.g.C;
+    float2 *grid = D.grid;
+    const long long top = 2LL * H * C, side = 2LL * H * n1;
+    for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < top + side;
+         idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int r, c;
+        if (idx < top) {
+            const int rr = static_cast<int>(idx / C);
+            c = static_cast<int>(idx - static_cast<long long>(rr) * C);
+            r = rr < H ? rr : rr + n1;
+        } else {
+            const long long j = idx - top;
+            r = H + static_cast<int>(j / (2 * H));
+            const int cc = static_cast<int>(j - static_cast<long long>(r - H) * 2 * H);
+            c = cc < H ? cc : cc + n2;
+        }
+        grid[static_cast<size_t>(r) * C + c] = grid[static_cast<size_t>(pmod(r - H, n1) + H) * C + pmod(c - H, n2) + H];
+    }
+}
+
+// Halo fold (type 1) of transform blockIdx.y: each interior cell within H of
+// an edge adds its periodic images.
+__global__ void k_batch_fold(const BatchDesc *__restrict__ d) {
+    const BatchDesc &D = d[blockIdx.y];
+    const int n1 = D.g.n1, n2 = D.g.n2, H = D.g.H, C = D.g.C, R = D.g.R, Cl = D.g.Cl;
+    float2 *grid = D.grid;
+    const int rows_tb = (n1 <= 2 * H) ? n1 : 2 * H;
+    const int cols_lr = (n2 <= 2 * H) ? n2 : 2 * H;
+    const long long part1 = static_cast<long long>(rows_tb) * n2;
+    const long long part2 = (n1 > 2 * H) ? static_cast<long long>(n1 - 2 * H) * cols_lr : 0;
+    for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < part1 + part2;
+         idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int r, c;
+        if (idx < part1) {
+            const int rr = static_cast<int>(idx / n2);
+            c = static_cast<int>(idx - static_cast<long long>(rr) * n2);
+            r = (n1 <= 2 * H) ? rr : (rr < H ? rr : n1 - 2 * H + rr);
+        } else {
+            const long long j = idx - part1;
+            const int rr = static_cast<int>(j / cols_lr);
+            const int cc = static_cast<int>(j - static_cast<long long>(rr) * cols_lr);
+            r = H + rr;
+            c = (n2 <= 2 * H) ? cc : (cc < H ? cc : n2 - 2 * H + cc);
+        }
+        const int pr0 = r + H, pc0 = c + H;
+        const int amin = -(pr0 / n1), amax = (R - 1 - pr0) / n1;
+        const int bmin = -(pc0 / n2), bmax = (Cl - 1 - pc0) / n2;
+        float2 acc = grid[static_cast<size_t>(pr0) * C + pc0];
+        for (int a = amin; a <= amax; ++a)
+            for (int b = bmin; b <= bmax; ++b) {
+                if (a == 0 && b == 0) continue;
+                const float2 v = grid[static_cast<size_t>(pr0 + a * n1) * C + (pc0 + b * n2)];
+                acc.x += v.x;
+                acc.y += v.y;
+            }
+        grid[static_cast<size_t>(pr0) * C + pc0] = acc;
+    }
+}
+
+// ---- persistent gather over the work items of all transforms --------------
+template <int K>
+__device__ __forceinline__ void batch_issue(const BatchDesc *__restrict__ d, int n, int gc, float2 *dst,
+                                            uint64_t *bar) {
+    const int t = find_transform<0>(d, n, gc);
+    const BatchDesc &D = d[t];
+    const int tile = __ldg(&D.chunks[gc - D.chunk_base].x);
+    const int tr = tile / D.g.tiles2, tc = tile - tr * D.g.tiles2;
+    mbar_arrive_expect_tx(bar, static_cast<uint32_t>(D.g.PR * D.g.PC * sizeof(float2)));
+    tma_load_2d(dst, &D.tmap, bar, 2 * (D.g.H + tc * D.g.T - D.g.Ke), D.g.H + tr * D.g.T - K);
+}
+
+template <int K, bool COMP>
+__global__ void __launch_bounds__(kThreads, 4)
+    k_batch_gather(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total, Geom g0,
+                   float alpha, float cn, float kp, int *status) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_ok;
+    const int pstride = patch_stride_elems(g0);  // the same for every transform (same T, K)
+    float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) < total) batch_issue<K>(d, n, blockIdx.x, bufs, &bars[0]);
+    uint32_t phase = 0;
+    int it = 0;
+    for (int gc = blockIdx.x; gc < total; gc += gridDim.x, ++it) {
+        const int b = it & 1;
+        const uint32_t par = (phase >> b) & 1u;
+        const int gnext = gc + gridDim.x;
+        if (threadIdx.x == 0) {
+            if (gnext < total) {
+                fence_proxy_async_smem();
+                batch_issue<K>(d, n, gnext, bufs + (b ^ 1) * pstride, &bars[b ^ 1]);
+            }
+            s_ok = mbar_wait_bounded(&bars[b], par) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_ok) {
+            if (threadIdx.x == 0) {
+                latch_error(status, kErrTimeout);
+                if (gnext < total) (void)mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+            }
+            return;
+        }
+        if (threadIdx.x != 0) (void)mbar_wait_bounded(&bars[b], par);
+        phase ^= (1u << b);
+
+        const int t = find_transform<0>(d, n, gc);
+        const BatchDesc &D = d[t];
+        const int4 ch = __ldg(&D.chunks[gc - D.chunk_base]);
+        const int tr = ch.x / D.g.tiles2, tc = ch.x - tr * D.g.tiles2;
+        const int r0 = tr * g0.T, c0 = tc * g0.T;
+        const float2 *patch = bufs + b * pstride;
+        const Rec32 *recs = D.recs;
+        float2 *out = io[t].out;
+        for (int i = threadIdx.x; i < ch.z; i += kThreads) {
+            const int4 raw = __ldg(reinterpret_cast<const int4 *>(recs) + ch.y + i);
+            const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
+            const int lr = mu1 - r0, lc = mu2 - c0;
+            if (static_cast<unsigned>(lr) >= static_cast<unsigned>(g0.T) ||
+                static_cast<unsigned>(lc) >= static_cast<unsigned>(g0.T)) {
+                latch_error(status, kErrBounds);
+                continue;
+            }
+            out[raw.w] = gather_point<K, COMP>(patch, g0.PC, g0.Ke, lr, lc, __int_as_float(raw.x),
+                                               __int_as_float(raw.y), alpha, cn, kp);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- persistent spread over the work items of all transforms --------------
+template <int K>
+__global__ void __launch_bounds__(kSpreadWarps * 32)
+    k_batch_spread(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total, Geom g0,
+                   float alpha, float cn, float kp, int chunk, int *work, int *status) {
+    extern __shared__ unsigned char smem_raw[];
+    constexpr int PR = kRegTile + 2 * K;
+    constexpr int SP = point_scratch<K>();
+    float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pstride = patch_stride_elems(g0);
+    float2 *patch = bufs + warp * pstride;
+    float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * SP;
+    const int parts = (chunk + kSpreadItem - 1) / kSpreadItem;
+    bool pending = false;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(work, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total * parts) break;
+        const int gc = item / parts, part = item - gc * parts;
+        const int t = find_transform<0>(d, n, gc);
+        const BatchDesc &D = d[t];
+        int4 ch = __ldg(&D.chunks[gc - D.chunk_base]);
+        const int first = part * kSpreadItem;
+        if (first >= ch.z) continue;
+        ch.y += first;
+        ch.z = min(kSpreadItem, ch.z - first);
+        const int tr = ch.x / D.g.tiles2, tc = ch.x - tr * D.g.tiles2;
+        const int r0 = tr * kRegTile, c0 = tc * kRegTile;
+        float2 acc[PR];
+#pragma unroll
+        for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
+        spread_points<K>(D.recs, ch.y, ch.z, r0, c0, io[t].in, scr, acc, alpha, cn, kp, status);
+        flush_patch<K>(&D.tmap, patch, acc, g0.H, r0, c0, pending);
+        pending = true;
+    }
+    if (lane == 0) bulk_wait_all();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host object
+// ---------------------------------------------------------------------------
+struct nfft2d_batch_s {
+    int count = 0, K = 6;
+    double sigma = 2.0;
+    cudaStream_t user_stream = nullptr;
+    cudaStream_t stream = nullptr;  // the batch's own stream (captured into graphs)
+    std::vector<nfft2d_plan_s *> plans;
+    void *grids = nullptr;
+    size_t grid_bytes = 0;
+    struct Group {
+        int N1, N2;
+        std::vector<int> members;  // transform indices, contiguous in `grids`
+        size_t first_elem = 0;     // element offset of the first member's grid
+        cufftHandle fft = 0;
+        bool fft_ok = false;
+    };
+    std::vector<Group> groups;
+    BatchDesc *d_desc = nullptr;
+    BatchIO *d_io = nullptr;
+    BatchIO *h_io = nullptr;  // pinned
+    int *d_work = nullptr;    // spread work counter
+    int *d_status = nullptr;  // [1] error bits (shared by the batched kernels)
+    int total_chunks = 0, total_rows = 0, total_crop = 0;
+    bool points_valid = false;
+    bool use_graph = true;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0] type-2 forward, [1] type-1 adjoint
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_io = nullptr;
+    bool io_pending = false;
+    Geom g0{};
+    float alpha = 0, cn = 0, kp = 0;
+};
+
+namespace {
+
+void batch_free(nfft2d_batch_s *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (auto &gx : b->graph)
+        if (gx) cudaGraphExecDestroy(gx);
+    for (auto &gr : b->groups)
+        if (gr.fft_ok) cufftDestroy(gr.fft);
+    for (auto *p : b->plans) release_plan(p);
+    cudaFree(b->grids);
+    cudaFree(b->d_desc);
+    cudaFree(b->d_io);
+    cudaFreeHost(b->h_io);
+    cudaFree(b->d_work);
+    cudaFree(b->d_status);
+    for (auto e : {b->ev_in, b->ev_out, b->ev_io})
+        if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int status_of(cudaError_t e) {
+    if (e == cudaSuccess) return NFFT2D_OK;
+    return e == cudaErrorMemoryAllocation ? NFFT2D_ERR_OOM : NFFT2D_ERR_CUDA;
+}
+
+#define B_TRY(expr)                                   \
+    do {                                              \
+        cudaError_t e_ = (expr);                      \
+        if (e_ != cudaSuccess) return status_of(e_);  \
+    } while (0)
+
+void drop_graphs(nfft2d_batch_s *b) {
+    for (auto &gx : b->graph)
+        if (gx) {
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
+        }
+}
+
+int run_ffts(nfft2d_batch_s *b, int dir) {
+    for (auto &gr : b->groups) {
+        const Geom &g = b->plans[gr.members[0]]->g;
+        cufftComplex *base = static_cast<cufftComplex *>(b->grids) + gr.first_elem + static_cast<size_t>(g.H) * g.C + g.H;
+        if (cufftExecC2C(gr.fft, base, base, dir) != CUFFT_SUCCESS) return NFFT2D_ERR_CUFFT;
+    }
+    return NFFT2D_OK;
+}
+
+template <int K>
+int enqueue_stages(nfft2d_batch_s *b, int type) {
+    const int n = b->count;
+    const Geom &g0 = b->g0;
+    const int pstride = patch_stride_elems(g0);
+    int per_sm = 0, sms = 0, dev = 0;
+    B_TRY(cudaGetDevice(&dev));
+    B_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (type == 2) {
+        k_batch_pad<<<b->total_rows, kThreads, 0, b->stream>>>(b->d_desc, n, b->d_io);
+        B_TRY(cudaGetLastError());
+        int st = run_ffts(b, CUFFT_FORWARD);
+        if (st != NFFT2D_OK) return st;
+        k_batch_fill<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
+        B_TRY(cudaGetLastError());
+        if (b->total_chunks > 0) {
+            const int smem = 2 * pstride * static_cast<int>(sizeof(float2)) + 128;
+            auto kernel = k_batch_gather<K, true>;
+            if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem));
+            const int blocks = std::max(1, std::min(b->total_chunks, std::max(per_sm, 1) * sms));
+            kernel<<<blocks, kThreads, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0, b->alpha, b->cn,
+                                                          b->kp, b->d_status);
+            B_TRY(cudaGetLastError());
+        }
+    } else {
+        B_TRY(cudaMemsetAsync(b->grids, 0, b->grid_bytes, b->stream));
+        if (b->total_chunks > 0) {
+            const int smem = kSpreadWarps * pstride * static_cast<int>(sizeof(float2)) + 128 +
+                             kSpreadWarps * 32 * point_scratch<K>() * static_cast<int>(sizeof(float));
+            auto kernel = k_batch_spread<K>;
+            if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSpreadWarps * 32, smem));
+            const int chunk = b->plans[0]->chunk;
+            const long long items = static_cast<long long>(b->total_chunks) * ((chunk + kSpreadItem - 1) / kSpreadItem);
+            const int blocks = static_cast<int>(std::max(1LL, std::min<long long>((items + kSpreadWarps - 1) / kSpreadWarps,
+                                                                            std::max(per_sm, 1) * sms)));
+            B_TRY(cudaMemsetAsync(b->d_work, 0, sizeof(int), b->stream));
+            kernel<<<blocks, kSpreadWarps * 32, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0, b->alpha,
+                                                                   b->cn, b->kp, chunk, b->d_work, b->d_status);
+            B_TRY(cudaGetLastError());
+        }
+        k_batch_fold<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
+        B_TRY(cudaGetLastError());
+        int st = run_ffts(b, CUFFT_INVERSE);
+        if (st != NFFT2D_OK) return st;
+        k_batch_crop<<<b->total_crop, kThreads, 0, b->stream>>>(b->d_desc, n, b->d_io);
+        B_TRY(cudaGetLastError());
+    }
+    return NFFT2D_OK;
+}
+
+int enqueue(nfft2d_batch_s *b, int type) {
+    switch (b->K) {
+        case 2: return enqueue_stages<2>(b, type);
+        case 3: return enqueue_stages<3>(b, type);
+        case 4: return enqueue_stages<4>(b, type);
+        case 5: return enqueue_stages<5>(b, type);
+        case 6: return enqueue_stages<6>(b, type);
+        case 7: return enqueue_stages<7>(b, type);
+        case 8: return enqueue_stages<8>(b, type);
+        default: return NFFT2D_ERR_INVALID_ARG;
+    }
+}
+
+int run(nfft2d_batch_s *b, int type, const void *const *in, void *const *out) {
+    if (!b || !in || !out) return NFFT2D_ERR_INVALID_ARG;
+    if (!b->points_valid) return NFFT2D_ERR_NO_POINTS;
+    // the point-side array of a transform with no points may be null
+    for (int t = 0; t < b->count; ++t) {
+        const bool empty = b->plans[t]->M == 0;
+        const void *coef = type == 2 ? in[t] : out[t];
+        const void *pts = type == 2 ? out[t] : in[t];
+        if (!coef || (!pts && !empty)) return NFFT2D_ERR_INVALID_ARG;
+    }
+    // the previous copy of the pointer table must have left the pinned buffer
+    if (b->io_pending) B_TRY(cudaEventSynchronize(b->ev_io));
+    for (int t = 0; t < b->count; ++t) {
+        b->h_io[t].in = static_cast<const float2 *>(in[t]);
+        b->h_io[t].out = static_cast<float2 *>(out[t]);
+    }
+    B_TRY(cudaEventRecord(b->ev_in, b->user_stream));
+    B_TRY(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
+    B_TRY(cudaMemcpyAsync(b->d_io, b->h_io, sizeof(BatchIO) * b->count, cudaMemcpyHostToDevice, b->stream));
+    B_TRY(cudaEventRecord(b->ev_io, b->stream));
+    b->io_pending = true;
+    const int gi = type == 2 ? 0 : 1;
+    if (b->use_graph) {
+        if (!b->graph[gi]) {
+            cudaGraph_t graph = nullptr;
+            B_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            const int st = enqueue(b, type);
+            const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
+            if (st != NFFT2D_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            B_TRY(ec);
+            const cudaError_t ei = cudaGraphInstantiate(&b->graph[gi], graph, 0);
+            cudaGraphDestroy(graph);
+            B_TRY(ei);
+        }
+        B_TRY(cudaGraphLaunch(b->graph[gi], b->stream));
+    } else {
+        const int st = enqueue(b, type);
+        if (st != NFFT2D_OK) return st;
+    }
+    B_TRY(cudaEventRecord(b->ev_out, b->stream));
+    B_TRY(cudaStreamWaitEvent(b->user_stream, b->ev_out, 0));
+    return NFFT2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *N2, double sigma, int K,
+                        void *stream) {
+    if (!out || count <= 0 || !N1 || !N2) return NFFT2D_ERR_INVALID_ARG;
+    *out = nullptr;
+    for (int t = 0; t < count; ++t) {
+        Geom g{};
+        const int st = compute_layout(N1[t], N2[t], sigma, K, NFFT2D_F32, kRegTile, &g, nullptr, nullptr);
+        if (st != NFFT2D_OK) return st;
+    }
+    nfft2d_batch_s *b = new (std::nothrow) nfft2d_batch_s();
+    if (!b) return NFFT2D_ERR_OOM;
+    auto fail = [&](int s) {
+        batch_free(b);
+        return s;
+    };
+    b->count = count;
+    b->K = K;
+    b->sigma = sigma;
+    b->user_stream = static_cast<cudaStream_t>(stream);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    for (auto *e : {&b->ev_in, &b->ev_out, &b->ev_io})
+        if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+
+    // group by size; lay the grids out group by group
+    std::map<std::pair<int, int>, std::vector<int>> by_size;
+    for (int t = 0; t < count; ++t) by_size[{N1[t], N2[t]}].push_back(t);
+    std::vector<size_t> offset(count);
+    size_t elems = 0;
+    for (auto &kv : by_size) {
+        nfft2d_batch_s::Group gr;
+        gr.N1 = kv.first.first;
+        gr.N2 = kv.first.second;
+        gr.members = kv.second;
+        Geom g{};
+        compute_layout(gr.N1, gr.N2, sigma, K, NFFT2D_F32, kRegTile, &g, nullptr, nullptr);
+        gr.first_elem = elems;
+        for (int t : gr.members) {
+            offset[t] = elems;
+            elems += static_cast<size_t>(g.Ra) * g.C;
+        }
+        b->groups.push_back(gr);
+    }
+    b->grid_bytes = elems * sizeof(float2);
+    if (cudaMalloc(&b->grids, b->grid_bytes) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMemsetAsync(b->grids, 0, b->grid_bytes, b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    b->plans.assign(count, nullptr);
+    for (int t = 0; t < count; ++t) {
+        const int st = create_plan(&b->plans[t], N1[t], N2[t], sigma, K, NFFT2D_F32, kRegTile, b->stream,
+                                   static_cast<float2 *>(b->grids) + offset[t]);
+        if (st != NFFT2D_OK) return fail(st);
+    }
+    for (auto &gr : b->groups) {
+        const Geom &g = b->plans[gr.members[0]]->g;
+        int nn[2] = {g.n1, g.n2}, emb[2] = {g.Ra, g.C};
+        const int dist = g.Ra * g.C;
+        if (cufftPlanMany(&gr.fft, 2, nn, emb, 1, dist, emb, 1, dist, CUFFT_C2C,
+                          static_cast<int>(gr.members.size())) != CUFFT_SUCCESS)
+            return fail(NFFT2D_ERR_CUFFT);
+        gr.fft_ok = true;
+        if (cufftSetStream(gr.fft, b->stream) != CUFFT_SUCCESS) return fail(NFFT2D_ERR_CUFFT);
+    }
+    if (cudaMalloc(&b->d_desc, sizeof(BatchDesc) * count) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMalloc(&b->d_io, sizeof(BatchIO) * count) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMallocHost(&b->h_io, sizeof(BatchIO) * count) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMalloc(&b->d_work, sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMalloc(&b->d_status, 4 * sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMemsetAsync(b->d_status, 0, 4 * sizeof(int), b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    b->g0 = b->plans[0]->g;
+    b->alpha = static_cast<float>(b->plans[0]->w.alpha);
+    b->cn = static_cast<float>(b->plans[0]->w.cn);
+    b->kp = static_cast<float>(b->plans[0]->w.kp);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    *out = b;
+    return NFFT2D_OK;
+}
+
+int nfft2d_batch_destroy(nfft2d_batch b) {
+    if (!b) return NFFT2D_ERR_INVALID_ARG;
+    batch_free(b);
+    return NFFT2D_OK;
+}
+
+int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *const *x1, const void *const *x2,
+                            int coord_dtype, int units) {
+    if (!b || !M || !x1 || !x2) return NFFT2D_ERR_INVALID_ARG;
+    b->points_valid = false;
+    drop_graphs(b);
+    B_TRY(cudaStreamSynchronize(b->stream));
+    std::vector<BatchDesc> h(b->count);
+    int chunks = 0, rows = 0, crop = 0;
+    for (int t = 0; t < b->count; ++t) {
+        nfft2d_plan_s *p = b->plans[t];
+        const int st = nfft2d_set_points(p, M[t], x1[t], x2[t], coord_dtype, units);
+        if (st != NFFT2D_OK) return st;
+        BatchDesc &D = h[t];
+        std::memset(&D, 0, sizeof(D));
+        std::memcpy(&D.tmap, &p->tmap, sizeof(CUtensorMap));
+        D.recs = static_cast<const Rec32 *>(p->recs);
+        D.chunks = p->chunks;
+        D.grid = static_cast<float2 *>(p->grid);
+        D.deap1 = static_cast<const float *>(p->deap1);
+        D.deap2 = static_cast<const float *>(p->deap2);
+        D.g = p->g;
+        D.N1 = p->N1;
+        D.N2 = p->N2;
+        D.n_chunks = static_cast<int>(p->n_chunks);
+        D.chunk_base = chunks;
+        D.row_base = rows;
+        D.crop_base = crop;
+        D.chunk = p->chunk;
+        chunks += D.n_chunks;
+        rows += p->g.n1;
+        crop += p->N1;
+    }
+    B_TRY(cudaMemcpy(b->d_desc, h.data(), sizeof(BatchDesc) * b->count, cudaMemcpyHostToDevice));
+    b->total_chunks = chunks;
+    b->total_rows = rows;
+    b->total_crop = crop;
+    b->points_valid = true;
+    return NFFT2D_OK;
+}
+
+int nfft2d_batch_forward(nfft2d_batch b, const void *const *F, void *const *f) { return run(b, 2, F, f); }
+
+int nfft2d_batch_adjoint(nfft2d_batch b, const void *const *f, void *const *F) { return run(b, 1, f, F); }
+
+int nfft2d_batch_set_graph(nfft2d_batch b, int on) {
+    if (!b) return NFFT2D_ERR_INVALID_ARG;
+    b->use_graph = on != 0;
+    if (!b->use_graph) drop_graphs(b);
+    return NFFT2D_OK;
+}
+
+int nfft2d_batch_synchronize(nfft2d_batch b) {
+    if (!b) return NFFT2D_ERR_INVALID_ARG;
+    int hs[4] = {0, 0, 0, 0};
+    B_TRY(cudaStreamSynchronize(b->stream));
+    B_TRY(cudaMemcpy(hs, b->d_status, sizeof(hs), cudaMemcpyDeviceToHost));
+    if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
+    if (hs[1] & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
+    return NFFT2D_OK;
+}
+
+}  // extern "C"

@@ -22,6 +22,7 @@
 #include "nfft2d_device.cuh"
 #include "nfft2d_internal.h"
 #include "nfft2d_kargs.cuh"
+#include "nfft2d_tile_ops.cuh"
 
 namespace nfft2d {
 namespace {
@@ -40,7 +41,9 @@ __device__ __forceinline__ void issue_patch(const CUtensorMap *map, const int4 *
 }
 
 // MODE 0: f = gather(grid);  MODE 1: coordinate gradient contracted with vin.
-template <int K, bool COMP, int MODE>
+// CPC > 0 fixes the patch pitch at compile time (all tap loads then use
+// immediate offsets); CPC = 0 reads it from the geometry.
+template <int K, bool COMP, int MODE, int CPC>
 __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(const __grid_constant__ CUtensorMap tmap,
                                                            const Rec32 *__restrict__ recs,
                                                            const int4 *__restrict__ chunks, float2 *__restrict__ out,
@@ -51,6 +54,7 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
     __shared__ int s_ok;
     constexpr int W = 2 * K + 1;
     const Geom g = a.g;
+    const int PC = CPC > 0 ? CPC : g.PC;
     const int pstride = patch_stride_elems(g);
     // TMA shared-memory operands: 128-byte aligned (the launch adds 128 bytes of slack)
     float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -102,42 +106,19 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                 latch_error(a.status, kErrBounds);
                 continue;
             }
-            float w1[W], w2[W];
-            weights_f32<K>(t1, w1, a.alpha, a.cn, a.kp);
-            weights_f32<K>(t2, w2, a.alpha, a.cn, a.kp);
-            const float2 *base = patch + lr * g.PC + lc + (g.Ke - K);
             if (MODE == 0) {
-                float sx = 0.f, sy = 0.f, ex = 0.f, ey = 0.f;
-#pragma unroll
-                for (int r = 0; r < W; ++r) {
-                    const float2 *row = base + r * g.PC;
-                    float rx = 0.f, ry = 0.f;
-#pragma unroll
-                    for (int q = 0; q < W; ++q) {
-                        const float2 v = row[q];
-                        rx = fmaf(w2[q], v.x, rx);
-                        ry = fmaf(w2[q], v.y, ry);
-                    }
-                    if (COMP) {
-                        float e;
-                        two_sum(sx, __fmul_rn(w1[r], rx), sx, e);
-                        ex = __fadd_rn(ex, e);
-                        two_sum(sy, __fmul_rn(w1[r], ry), sy, e);
-                        ey = __fadd_rn(ey, e);
-                    } else {
-                        sx = fmaf(w1[r], rx, sx);
-                        sy = fmaf(w1[r], ry, sy);
-                    }
-                }
-                out[raw.w] = make_float2(sx + ex, sy + ey);
+                out[raw.w] = gather_point<K, COMP>(patch, PC, g.Ke, lr, lc, t1, t2, a.alpha, a.cn, a.kp);
             } else {
-                float d1[W], d2[W];
+                float w1[W], w2[W], d1[W], d2[W];
+                weights_f32<K>(t1, w1, a.alpha, a.cn, a.kp);
+                weights_f32<K>(t2, w2, a.alpha, a.cn, a.kp);
+                const float2 *base = patch + lr * PC + lc + (g.Ke - K);
                 dweights_f32<K>(t1, w1, d1, a.alpha, a.cn);
                 dweights_f32<K>(t2, w2, d2, a.alpha, a.cn);
                 float ax = 0.f, ay = 0.f, bx = 0.f, by = 0.f;
 #pragma unroll
                 for (int r = 0; r < W; ++r) {
-                    const float2 *row = base + r * g.PC;
+                    const float2 *row = base + r * PC;
                     float rx = 0.f, ry = 0.f, qx = 0.f, qy = 0.f;
 #pragma unroll
                     for (int q = 0; q < W; ++q) {
@@ -275,7 +256,9 @@ cudaError_t launch_K(const nfft2d_plan_s *p, void *f, const void *v, void *g1, v
     if (p->precision == NFFT2D_F32 && p->gather_variant == NFFT2D_VARIANT_TILED) {
         if (p->n_chunks == 0) return cudaSuccess;
         const int smem = 2 * patch_stride_elems(p->g) * static_cast<int>(sizeof(float2)) + 128;
-        auto kernel = p->compensated ? k_gather_tiled<K, true, MODE> : k_gather_tiled<K, false, MODE>;
+        auto kernel = p->g.PC == 32
+                          ? (p->compensated ? k_gather_tiled<K, true, MODE, 32> : k_gather_tiled<K, false, MODE, 32>)
+                          : (p->compensated ? k_gather_tiled<K, true, MODE, 0> : k_gather_tiled<K, false, MODE, 0>);
         cudaError_t e = prepare_smem(kernel, smem);
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kThreads, smem);

@@ -80,6 +80,7 @@ struct nfft2d_plan_s {
 
     // device buffers owned by the plan
     void *grid = nullptr;        // R*C complex, the padded oversampled grid
+    bool grid_external = false;  // grid owned by a batch (no free, no own cuFFT plan)
     void *deap1 = nullptr;       // N1 reals: S / phi(xi_k1), plan precision
     void *deap2 = nullptr;       // N2 reals
     int *d_status = nullptr;     // [0] n_chunks, [1] error bits
@@ -132,5 +133,14 @@ cudaError_t launch_spread(const nfft2d_plan_s *p, const void *f);
 int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1, int *n2);
 
 int grid_blocks(const nfft2d_plan_s *p, const void *kernel, int threads, int smem);
+
+// Plan creation shared by nfft2d_plan_create and batches.  With ext_grid set
+// the plan works on that (zeroed, Ra x C) grid instead of allocating one and
+// creates no cuFFT plan of its own (the batch runs the FFTs); tile = 0 picks
+// the default tile.
+int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int precision, int tile,
+                cudaStream_t stream, void *ext_grid);
+void release_plan(nfft2d_plan_s *p);
+int tensor_map_for(nfft2d_plan_s *p);
 
 }  // namespace nfft2d

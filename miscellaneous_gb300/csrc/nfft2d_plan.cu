@@ -461,7 +461,7 @@ void destroy_plan(nfft2d_plan_s *p) {
     if (!p) return;
     if (p->fft_ok) cufftDestroy(p->fft);
     free_points(p);
-    cudaFree(p->grid);
+    if (!p->grid_external) cudaFree(p->grid);
     cudaFree(p->deap1);
     cudaFree(p->deap2);
     cudaFree(p->d_status);
@@ -511,20 +511,22 @@ int setup_grid(nfft2d_plan_s *p) {
         cufftDestroy(p->fft);
         p->fft_ok = false;
     }
-    cudaFree(p->grid);
-    p->grid = nullptr;
     p->tmap_ok = false;
-    const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C;
-    NFFT_TRY_CUDA(cudaMalloc(&p->grid, bytes));
-    NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, bytes, p->stream));
-    int n[2] = {g.n1, g.n2};
-    int emb[2] = {g.Ra, g.C};
-    const int dist = g.Ra * g.C;
-    cufftResult fr = cufftPlanMany(&p->fft, 2, n, emb, 1, dist, emb, 1, dist,
-                                   p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C, 1);
-    if (fr != CUFFT_SUCCESS) return status_from_cufft(fr);
-    p->fft_ok = true;
-    if ((fr = cufftSetStream(p->fft, p->stream)) != CUFFT_SUCCESS) return status_from_cufft(fr);
+    if (!p->grid_external) {
+        cudaFree(p->grid);
+        p->grid = nullptr;
+        const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C;
+        NFFT_TRY_CUDA(cudaMalloc(&p->grid, bytes));
+        NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, bytes, p->stream));
+        int n[2] = {g.n1, g.n2};
+        int emb[2] = {g.Ra, g.C};
+        const int dist = g.Ra * g.C;
+        cufftResult fr = cufftPlanMany(&p->fft, 2, n, emb, 1, dist, emb, 1, dist,
+                                       p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C, 1);
+        if (fr != CUFFT_SUCCESS) return status_from_cufft(fr);
+        p->fft_ok = true;
+        if ((fr = cufftSetStream(p->fft, p->stream)) != CUFFT_SUCCESS) return status_from_cufft(fr);
+    }
     if (p->precision == NFFT2D_F32) return make_tensor_map(p);
     return NFFT2D_OK;
 }
@@ -753,11 +755,16 @@ int nfft2d_layout_query(int N1, int N2, double sigma, int K, int precision, int 
     return NFFT2D_OK;
 }
 
-int nfft2d_plan_create(nfft2d_plan *out, int N1, int N2, double sigma, int K, int precision, void *stream) {
+}  // extern "C"
+
+namespace nfft2d {
+
+int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int precision, int tile,
+                cudaStream_t stream, void *ext_grid) {
     if (!out) return NFFT2D_ERR_INVALID_ARG;
     *out = nullptr;
     Geom g{};
-    int st = compute_layout(N1, N2, sigma, K, precision, 0, &g, nullptr, nullptr);
+    int st = compute_layout(N1, N2, sigma, K, precision, tile, &g, nullptr, nullptr);
     if (st != NFFT2D_OK) return st;
     nfft2d_plan_s *p = new (std::nothrow) nfft2d_plan_s();
     if (!p) return NFFT2D_ERR_OOM;
@@ -767,7 +774,9 @@ int nfft2d_plan_create(nfft2d_plan *out, int N1, int N2, double sigma, int K, in
     p->sigma = sigma;
     p->precision = precision;
     p->g = g;
-    p->stream = static_cast<cudaStream_t>(stream);
+    p->stream = stream;
+    p->grid = ext_grid;
+    p->grid_external = ext_grid != nullptr;
     if (precision == NFFT2D_F64) {
         p->gather_variant = NFFT2D_VARIANT_DIRECT;
         p->spread_variant = NFFT2D_VARIANT_DIRECT;
@@ -824,6 +833,18 @@ int nfft2d_plan_create(nfft2d_plan *out, int N1, int N2, double sigma, int K, in
     p->workspace_bytes = plan_workspace_bytes(p);
     *out = p;
     return NFFT2D_OK;
+}
+
+void release_plan(nfft2d_plan_s *p) { destroy_plan(p); }
+
+int tensor_map_for(nfft2d_plan_s *p) { return make_tensor_map(p); }
+
+}  // namespace nfft2d
+
+extern "C" {
+
+int nfft2d_plan_create(nfft2d_plan *out, int N1, int N2, double sigma, int K, int precision, void *stream) {
+    return nfft2d::create_plan(out, N1, N2, sigma, K, precision, 0, static_cast<cudaStream_t>(stream), nullptr);
 }
 
 int nfft2d_plan_destroy(nfft2d_plan p) {

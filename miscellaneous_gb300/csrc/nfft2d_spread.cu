@@ -31,6 +31,7 @@
 #include "nfft2d_device.cuh"
 #include "nfft2d_internal.h"
 #include "nfft2d_kargs.cuh"
+#include "nfft2d_tile_ops.cuh"
 
 namespace nfft2d {
 namespace {
@@ -38,53 +39,7 @@ namespace {
 constexpr int kThreads = 256;
 
 constexpr int kSpreadWarps = 4;  // warps per CTA of the tiled spread
-constexpr int kRegTile = 16;     // tile edge the register-resident spread requires
 constexpr int kSpreadItem = 128; // points per warp work item (a chunk is split into items)
-// Per-point scratch (floats): lr, lc, v.x, v.y, then w1 and w2, each padded
-// to a multiple of 4 floats (2K+1 used).
-template <int K>
-constexpr int wpad() {
-    return ((2 * K + 1 + 3) / 4) * 4;
-}
-template <int K>
-constexpr int point_scratch() {
-    return 4 + 2 * wpad<K>();
-}
-
-// cp.async.bulk.wait_group.read 0: the warp's last reduction has finished
-// reading its shared-memory source.
-__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-
-// acc[L + a] += (ax, ay) * w1[a] for the 2K+1 rows of a point whose first
-// patch row is L (compile-time, so acc stays in registers).
-template <int K, int PR, int L>
-__device__ __forceinline__ void add_rows(float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax, float ay) {
-#pragma unroll
-    for (int a = 0; a <= 2 * K; ++a) {
-        acc[L + a].x = fmaf(ax, w1[a], acc[L + a].x);
-        acc[L + a].y = fmaf(ay, w1[a], acc[L + a].y);
-    }
-}
-
-// Dispatch on the point's first patch row with a jump table (the row offset
-// is warp-uniform, so every lane takes the same case).
-template <int K, int PR>
-__device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax,
-                                                float ay) {
-    static_assert(kRegTile == 16, "one case per row of a 16-row tile");
-#define NFFT2D_ROW_CASE(L)                          \
-    case L:                                         \
-        add_rows<K, PR, L>(acc, w1, ax, ay);        \
-        break;
-    switch (lr) {
-        NFFT2D_ROW_CASE(0) NFFT2D_ROW_CASE(1) NFFT2D_ROW_CASE(2) NFFT2D_ROW_CASE(3)
-        NFFT2D_ROW_CASE(4) NFFT2D_ROW_CASE(5) NFFT2D_ROW_CASE(6) NFFT2D_ROW_CASE(7)
-        NFFT2D_ROW_CASE(8) NFFT2D_ROW_CASE(9) NFFT2D_ROW_CASE(10) NFFT2D_ROW_CASE(11)
-        NFFT2D_ROW_CASE(12) NFFT2D_ROW_CASE(13) NFFT2D_ROW_CASE(14) NFFT2D_ROW_CASE(15)
-        default: break;
-    }
-#undef NFFT2D_ROW_CASE
-}
 
 template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid_constant__ CUtensorMap tmap,
@@ -92,16 +47,14 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
                                                                     const int4 *__restrict__ chunks,
                                                                     const float2 *__restrict__ f, const KArgs a) {
     extern __shared__ unsigned char smem_raw[];
-    constexpr int W = 2 * K + 1;
     constexpr int PR = kRegTile + 2 * K;  // patch rows
-    constexpr int KE = K + (K & 1);
     const Geom g = a.g;                   // g.T == kRegTile, g.PC == 32
     // TMA shared-memory operands: 128-byte aligned (the launch adds 128 bytes of slack)
     float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pstride = patch_stride_elems(g);
     float2 *patch = bufs + warp * pstride;  // this warp's flush buffer, PR x 32
-    constexpr int SP = point_scratch<K>(), WP = wpad<K>();
+    constexpr int SP = point_scratch<K>();
     float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * SP;
     const int n = a.n_chunks;
     int *work = a.status + 2;  // work-item counter, zeroed before the launch
@@ -125,63 +78,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
         float2 acc[PR];
 #pragma unroll
         for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
-
-        for (int base0 = 0; base0 < ch.z; base0 += 32) {
-            const int nb = min(32, ch.z - base0);
-            // 1) each lane prepares one point: offsets, value, 2(2K+1) weights
-            if (lane < nb) {
-                const int4 raw = __ldg(reinterpret_cast<const int4 *>(recs) + ch.y + base0 + lane);
-                const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
-                int lr = mu1 - r0, lc = mu2 - c0;
-                float2 v = __ldg(&f[raw.w]);
-                if (static_cast<unsigned>(lr) >= static_cast<unsigned>(kRegTile) ||
-                    static_cast<unsigned>(lc) >= static_cast<unsigned>(kRegTile)) {
-                    latch_error(a.status, kErrBounds);
-                    lr = lc = 0;
-                    v = make_float2(0.f, 0.f);  // contributes nothing
-                }
-                float w1[W], w2[W];
-                weights_f32<K>(__int_as_float(raw.x), w1, a.alpha, a.cn, a.kp);
-                weights_f32<K>(__int_as_float(raw.y), w2, a.alpha, a.cn, a.kp);
-                float *sp = scr + lane * SP;
-                reinterpret_cast<float4 *>(sp)[0] = make_float4(__int_as_float(lr), __int_as_float(lc), v.x, v.y);
-#pragma unroll
-                for (int k = 0; k < WP; ++k) sp[4 + k] = k < W ? w1[k] : 0.f;
-#pragma unroll
-                for (int k = 0; k < WP; ++k) sp[4 + WP + k] = k < W ? w2[k] : 0.f;
-            }
-            __syncwarp();
-            // 2) the warp walks the points; lane = patch column
-            for (int j = 0; j < nb; ++j) {
-                const float *sp = scr + j * SP;
-                const float4 meta = reinterpret_cast<const float4 *>(sp)[0];
-                const int lr = __float_as_int(meta.x), lc = __float_as_int(meta.y);
-                float w1[WP];
-#pragma unroll
-                for (int q = 0; q < WP / 4; ++q) {
-                    const float4 t = reinterpret_cast<const float4 *>(sp + 4)[q];
-                    w1[4 * q] = t.x;
-                    w1[4 * q + 1] = t.y;
-                    w1[4 * q + 2] = t.z;
-                    w1[4 * q + 3] = t.w;
-                }
-                const int b = lane - lc - (KE - K);  // this lane's tap column
-                const float w2 = (static_cast<unsigned>(b) < static_cast<unsigned>(W)) ? sp[4 + WP + b] : 0.f;
-                add_rows_switch<K, PR>(lr, acc, w1, meta.z * w2, meta.w * w2);
-            }
-            __syncwarp();  // scratch is rewritten by the next batch
-        }
-        // 3) flush: registers -> shared patch -> one TMA reduce-add into the grid
-        if (lane == 0 && pending) bulk_wait_read_all();  // the last flush has read the patch
-        __syncwarp();
-#pragma unroll
-        for (int r = 0; r < PR; ++r) patch[r * 32 + lane] = acc[r];
-        fence_proxy_async_smem();  // generic-proxy writes -> visible to the TMA engine
-        __syncwarp();
-        if (lane == 0) {
-            tma_reduce_add_2d(&tmap, patch, 2 * (g.H + c0 - KE), g.H + r0 - K);
-            bulk_commit();
-        }
+        spread_points<K>(recs, ch.y, ch.z, r0, c0, f, scr, acc, a.alpha, a.cn, a.kp, a.status);
+        flush_patch<K>(&tmap, patch, acc, g.H, r0, c0, pending);
         pending = true;
     }
     if (lane == 0) bulk_wait_all();

@@ -1,0 +1,185 @@
+// nfft2d_tile_ops.cuh -- the per-point work of the tiled kernels, shared by the
+// single-transform kernels (nfft2d_gather.cu, nfft2d_spread.cu) and the
+// batched ones (nfft2d_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "nfft2d_device.cuh"
+#include "nfft2d_internal.h"
+
+namespace nfft2d {
+
+// ---------------------------------------------------------------------------
+// gather: one point from a shared-memory tile patch
+// ---------------------------------------------------------------------------
+
+// f = sum_{r,q} w1[r] w2[q] patch[lr + r][lc + (Ke - K) + q]; row partial sums
+// with FMA, the sum over rows compensated (TwoSum) when COMP.
+template <int K, bool COMP>
+__device__ __forceinline__ float2 gather_point(const float2 *__restrict__ patch, int PC, int Ke, int lr, int lc,
+                                               float t1, float t2, float alpha, float cn, float kp) {
+    constexpr int W = 2 * K + 1;
+    float w1[W], w2[W];
+    weights_f32<K>(t1, w1, alpha, cn, kp);
+    weights_f32<K>(t2, w2, alpha, cn, kp);
+    const float2 *base = patch + lr * PC + lc + (Ke - K);
+    float sx = 0.f, sy = 0.f, ex = 0.f, ey = 0.f;
+#pragma unroll
+    for (int r = 0; r < W; ++r) {
+        const float2 *row = base + r * PC;
+        float rx = 0.f, ry = 0.f;
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+            const float2 v = row[q];
+            rx = fmaf(w2[q], v.x, rx);
+            ry = fmaf(w2[q], v.y, ry);
+        }
+        if (COMP) {
+            float e;
+            two_sum(sx, __fmul_rn(w1[r], rx), sx, e);
+            ex = __fadd_rn(ex, e);
+            two_sum(sy, __fmul_rn(w1[r], ry), sy, e);
+            ey = __fadd_rn(ey, e);
+        } else {
+            sx = fmaf(w1[r], rx, sx);
+            sy = fmaf(w1[r], ry, sy);
+        }
+    }
+    return make_float2(sx + ex, sy + ey);
+}
+
+// ---------------------------------------------------------------------------
+// spread: a warp accumulates a 16 x 16 tile's (16+2K) x 32 patch in registers
+// ---------------------------------------------------------------------------
+constexpr int kRegTile = 16;  // tile edge the register-resident spread requires
+
+// Per-point scratch (floats): lr, lc, v.x, v.y, then w1 and w2, each padded
+// to a multiple of 4 floats (2K+1 used).
+template <int K>
+constexpr int wpad() {
+    return ((2 * K + 1 + 3) / 4) * 4;
+}
+template <int K>
+constexpr int point_scratch() {
+    return 4 + 2 * wpad<K>();
+}
+
+// acc[L + a] += (ax, ay) * w1[a] for the 2K+1 rows of a point whose first
+// patch row is L (compile-time, so acc stays in registers).
+template <int K, int PR, int L>
+__device__ __forceinline__ void add_rows(float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax, float ay) {
+#pragma unroll
+    for (int a = 0; a <= 2 * K; ++a) {
+        acc[L + a].x = fmaf(ax, w1[a], acc[L + a].x);
+        acc[L + a].y = fmaf(ay, w1[a], acc[L + a].y);
+    }
+}
+
+// Dispatch on the point's first patch row with a jump table (the row offset
+// is warp-uniform, so every lane takes the same case).
+template <int K, int PR>
+__device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax,
+                                                float ay) {
+    static_assert(kRegTile == 16, "one case per row of a 16-row tile");
+#define NFFT2D_ROW_CASE(L)                   \
+    case L:                                  \
+        add_rows<K, PR, L>(acc, w1, ax, ay); \
+        break;
+    switch (lr) {
+        NFFT2D_ROW_CASE(0) NFFT2D_ROW_CASE(1) NFFT2D_ROW_CASE(2) NFFT2D_ROW_CASE(3)
+        NFFT2D_ROW_CASE(4) NFFT2D_ROW_CASE(5) NFFT2D_ROW_CASE(6) NFFT2D_ROW_CASE(7)
+        NFFT2D_ROW_CASE(8) NFFT2D_ROW_CASE(9) NFFT2D_ROW_CASE(10) NFFT2D_ROW_CASE(11)
+        NFFT2D_ROW_CASE(12) NFFT2D_ROW_CASE(13) NFFT2D_ROW_CASE(14) NFFT2D_ROW_CASE(15)
+        default: break;
+    }
+#undef NFFT2D_ROW_CASE
+}
+
+// Add the contributions of points [first, first + cnt) of one tile (origin
+// r0, c0) to the warp's register patch acc (lane = patch column).  scr is the
+// warp's scratch of 32 * point_scratch<K>() floats.  A record outside the tile
+// latches kErrBounds and contributes nothing.
+template <int K>
+__device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, int first, int cnt, int r0, int c0,
+                                              const float2 *__restrict__ f, float *scr,
+                                              float2 (&acc)[kRegTile + 2 * K], float alpha, float cn, float kp,
+                                              int *status) {
+    constexpr int W = 2 * K + 1;
+    constexpr int PR = kRegTile + 2 * K;
+    constexpr int KE = K + (K & 1);
+    constexpr int SP = point_scratch<K>(), WP = wpad<K>();
+    const int lane = threadIdx.x & 31;
+    for (int base0 = 0; base0 < cnt; base0 += 32) {
+        const int nb = min(32, cnt - base0);
+        // 1) each lane prepares one point: offsets, value, 2(2K+1) weights
+        if (lane < nb) {
+            const int4 raw = __ldg(reinterpret_cast<const int4 *>(recs) + first + base0 + lane);
+            const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
+            int lr = mu1 - r0, lc = mu2 - c0;
+            float2 v = __ldg(&f[raw.w]);
+            if (static_cast<unsigned>(lr) >= static_cast<unsigned>(kRegTile) ||
+                static_cast<unsigned>(lc) >= static_cast<unsigned>(kRegTile)) {
+                latch_error(status, kErrBounds);
+                lr = lc = 0;
+                v = make_float2(0.f, 0.f);  // contributes nothing
+            }
+            float w1[W], w2[W];
+            weights_f32<K>(__int_as_float(raw.x), w1, alpha, cn, kp);
+            weights_f32<K>(__int_as_float(raw.y), w2, alpha, cn, kp);
+            float *sp = scr + lane * SP;
+            reinterpret_cast<float4 *>(sp)[0] = make_float4(__int_as_float(lr), __int_as_float(lc), v.x, v.y);
+#pragma unroll
+            for (int k = 0; k < WP; ++k) sp[4 + k] = k < W ? w1[k] : 0.f;
+#pragma unroll
+            for (int k = 0; k < WP; ++k) sp[4 + WP + k] = k < W ? w2[k] : 0.f;
+        }
+        __syncwarp();
+        // 2) the warp walks the points; lane = patch column
+        for (int j = 0; j < nb; ++j) {
+            const float *sp = scr + j * SP;
+            const float4 meta = reinterpret_cast<const float4 *>(sp)[0];
+            const int lr = __float_as_int(meta.x), lc = __float_as_int(meta.y);
+            float w1[WP];
+#pragma unroll
+            for (int q = 0; q < WP / 4; ++q) {
+                const float4 t = reinterpret_cast<const float4 *>(sp + 4)[q];
+                w1[4 * q] = t.x;
+                w1[4 * q + 1] = t.y;
+                w1[4 * q + 2] = t.z;
+                w1[4 * q + 3] = t.w;
+            }
+            const int b = lane - lc - (KE - K);  // this lane's tap column
+            const float w2 = (static_cast<unsigned>(b) < static_cast<unsigned>(W)) ? sp[4 + WP + b] : 0.f;
+            add_rows_switch<K, PR>(lr, acc, w1, meta.z * w2, meta.w * w2);
+        }
+        __syncwarp();  // scratch is rewritten by the next batch
+    }
+}
+
+// cp.async.bulk.wait_group.read 0: the thread's last bulk reduction has
+// finished reading its shared-memory source.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Flush a warp's register patch: lanes -> shared patch (PR x 32) -> one TMA
+// tensor reduction into the grid at the tile (r0, c0).  `pending` tells
+// whether the warp's previous flush may still be reading the patch.
+template <int K>
+__device__ __forceinline__ void flush_patch(const CUtensorMap *map, float2 *patch, const float2 (&acc)[kRegTile + 2 * K],
+                                            int H, int r0, int c0, bool pending) {
+    constexpr int PR = kRegTile + 2 * K;
+    constexpr int KE = K + (K & 1);
+    const int lane = threadIdx.x & 31;
+    if (lane == 0 && pending) bulk_wait_read_all();
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < PR; ++r) patch[r * 32 + lane] = acc[r];
+    fence_proxy_async_smem();  // generic-proxy writes -> visible to the TMA engine
+    __syncwarp();
+    if (lane == 0) {
+        tma_reduce_add_2d(map, patch, 2 * (H + c0 - KE), H + r0 - K);
+        bulk_commit();
+    }
+}
+
+}  // namespace nfft2d

@@ -186,6 +186,85 @@ class Plan:
         return g1, g2
 
 
+class Batch:
+    """Many FP32 transforms of uneven size run together (nfft2d_batch_*):
+    one batched cuFFT call per size group, one launch per stage for all
+    transforms, the whole stage sequence replayed as a CUDA graph."""
+
+    def __init__(self, sizes, sigma: float = 2.0, K: int = 6, stream: torch.cuda.Stream | None = None,
+                 graph: bool = True):
+        self._lib = _lib.load()
+        self.sizes = [(int(a), int(b)) for a, b in sizes]
+        self.count = len(self.sizes)
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        n1 = (ctypes.c_int * self.count)(*[a for a, _ in self.sizes])
+        n2 = (ctypes.c_int * self.count)(*[b for _, b in self.sizes])
+        h = ctypes.c_void_p()
+        check(self._lib.nfft2d_batch_create(ctypes.byref(h), self.count, n1, n2, float(sigma), int(K),
+                                            ctypes.c_void_p(self.stream.cuda_stream)), "nfft2d_batch_create")
+        self._h = h
+        self.M = [0] * self.count
+        self._keep = ()
+        if not graph:
+            check(self._lib.nfft2d_batch_set_graph(self._h, 0), "nfft2d_batch_set_graph")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.nfft2d_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def _ptrs(ts):
+        return (ctypes.c_void_p * len(ts))(*[t.data_ptr() for t in ts])
+
+    def set_points(self, x1s, x2s, units: str = "unit") -> None:
+        if len(x1s) != self.count or len(x2s) != self.count:
+            raise ValueError("one coordinate pair per transform")
+        dt = x1s[0].dtype
+        for a, b in zip(x1s, x2s):
+            _require_cuda(a, "x1", dt)
+            _require_cuda(b, "x2", dt)
+            if a.shape != b.shape:
+                raise ValueError("x1 and x2 must match")
+        M = (ctypes.c_longlong * self.count)(*[a.numel() for a in x1s])
+        cd = _lib.COORD_F32 if dt == torch.float32 else _lib.COORD_F64
+        check(self._lib.nfft2d_batch_set_points(self._h, M, self._ptrs(x1s), self._ptrs(x2s), cd, _lib.UNITS[units]),
+              "nfft2d_batch_set_points")
+        self.M = [a.numel() for a in x1s]
+        self._keep = (list(x1s), list(x2s))
+
+    def forward(self, Fs, outs=None):
+        for (n1, n2), F in zip(self.sizes, Fs):
+            _require_cuda(F, "F", torch.complex64, n1 * n2)
+        if outs is None:
+            outs = [torch.empty(m, dtype=torch.complex64, device=Fs[0].device) for m in self.M]
+        check(self._lib.nfft2d_batch_forward(self._h, self._ptrs(Fs), self._ptrs(outs)), "nfft2d_batch_forward")
+        return outs
+
+    def adjoint(self, fs, outs=None):
+        for m, f in zip(self.M, fs):
+            _require_cuda(f, "f", torch.complex64, m)
+        if outs is None:
+            outs = [torch.empty(n1 * n2, dtype=torch.complex64, device=fs[0].device) for n1, n2 in self.sizes]
+        check(self._lib.nfft2d_batch_adjoint(self._h, self._ptrs(fs), self._ptrs(outs)), "nfft2d_batch_adjoint")
+        return outs
+
+    def synchronize(self) -> None:
+        check(self._lib.nfft2d_batch_synchronize(self._h), "nfft2d_batch_synchronize")
+
+
 # ---------------------------------------------------------------------------
 # Reference call surface (c = 2, K = 6, grid-unit coordinates)
 # ---------------------------------------------------------------------------
@@ -293,5 +372,5 @@ def NDFT2_2D(data: torch.Tensor, x: torch.Tensor, y: torch.Tensor, N: int, M: in
     return out.view(N, M)
 
 
-__all__ = ["Plan", "NFFT2DError", "NFFT2_2D", "NFFT1_2D", "NDFT2_2D", "NFFT2_2D_GPU", "NDFT2_2D_GPU",
+__all__ = ["Plan", "Batch", "NFFT2DError", "NFFT2_2D", "NFFT1_2D", "NDFT2_2D", "NFFT2_2D_GPU", "NDFT2_2D_GPU",
            "Calculate_cuFFT_plan_C2C_NFFT2_2D", "Calculate_cuFFT_plan_Z2Z_NFFT2_2D", "Destroy_cuFFT_plan_NFFT2_2D"]

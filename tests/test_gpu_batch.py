@@ -1,0 +1,70 @@
+"""Batches (nfft2d_batch_*): many transforms of uneven size, one launch per
+stage, CUDA-graph replay.  Each transform of a batch must match the same
+transform run alone on a plan (same kernels, same binning): rel-L2 <= 1e-6;
+and the exact NDFT at the FP32 bar, rel-L2 <= 1e-5."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(sizes, Ms, seed):
+    rng = np.random.default_rng(seed)
+    xs, Fs, fs = [], [], []
+    for (n1, n2), m in zip(sizes, Ms):
+        xs.append((rng.uniform(-0.5, 0.5, m).astype(np.float32), rng.uniform(-0.5, 0.5, m).astype(np.float32)))
+        Fs.append((rng.standard_normal((n1, n2)) + 1j * rng.standard_normal((n1, n2))).astype(np.complex64))
+        fs.append((rng.standard_normal(m) + 1j * rng.standard_normal(m)).astype(np.complex64))
+    return xs, Fs, fs
+
+
+def _single(n1, n2, x, F, f):
+    from miscellaneous_gb300.nfft import Plan
+    with Plan(n1, n2) as p:
+        p.set_points(torch.from_numpy(x[0]).cuda(), torch.from_numpy(x[1]).cuda())
+        a = p.forward(torch.from_numpy(F).cuda().reshape(-1))
+        b = p.adjoint(torch.from_numpy(f).cuda())
+        p.synchronize()
+        return a.cpu().numpy(), b.cpu().numpy().reshape(-1)
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_matches_single_plans(orc, graph):
+    from miscellaneous_gb300.nfft import Batch
+    sizes = [(64, 64), (32, 48), (64, 64), (16, 16), (128, 64), (32, 48), (8, 8)]
+    Ms = [3000, 1, 500, 0, 7000, 257, 40]
+    with Batch(sizes, graph=graph) as bt:
+        for call, seed in enumerate((1, 2)):  # second call: new inputs, same points (graph replay)
+            xs, Fs, fs = _problem(sizes, Ms, 10)
+            rng = np.random.default_rng(seed)
+            Fs = [(rng.standard_normal(F.shape) + 1j * rng.standard_normal(F.shape)).astype(np.complex64) for F in Fs]
+            if call == 0:
+                bt.set_points([torch.from_numpy(x[0]).cuda() for x in xs], [torch.from_numpy(x[1]).cuda() for x in xs])
+            outs = bt.forward([torch.from_numpy(F).cuda().reshape(-1) for F in Fs])
+            adjs = bt.adjoint([torch.from_numpy(f).cuda() for f in fs])
+            bt.synchronize()
+            for t, ((n1, n2), x, F, f) in enumerate(zip(sizes, xs, Fs, fs)):
+                a, b = _single(n1, n2, x, F, f)
+                got_f, got_F = outs[t].cpu().numpy(), adjs[t].cpu().numpy()
+                if Ms[t] == 0:
+                    assert got_f.size == 0 and np.all(got_F == 0)
+                    continue
+                assert orc.rel_l2(got_f, a) < 1e-6, (call, t)
+                assert orc.rel_l2(got_F, b) < 1e-6, (call, t)
+                g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
+                assert orc.rel_l2(got_f, orc.ndft_type2(F, g1, g2, sign=-1)) < 1e-5, (call, t)
+
+
+def test_batch_rebinning_recaptures_the_graph(orc):
+    from miscellaneous_gb300.nfft import Batch
+    sizes = [(32, 32), (64, 32)]
+    with Batch(sizes) as bt:
+        for seed, Ms in ((3, [100, 900]), (4, [2000, 50])):
+            xs, Fs, fs = _problem(sizes, Ms, seed)
+            bt.set_points([torch.from_numpy(x[0]).cuda() for x in xs], [torch.from_numpy(x[1]).cuda() for x in xs])
+            outs = bt.forward([torch.from_numpy(F).cuda().reshape(-1) for F in Fs])
+            bt.synchronize()
+            for t, ((n1, n2), x, F) in enumerate(zip(sizes, xs, Fs)):
+                g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
+                assert orc.rel_l2(outs[t].cpu().numpy(), orc.ndft_type2(F, g1, g2, sign=-1)) < 1e-5

@@ -7,7 +7,10 @@ fallback.
 
 It wraps ``nfft2d_oracle.c`` (an FP64 C restatement of the reference's
 ``BP_FBP_FFBP/NFFT1_2D.m``, ``NFFT/NFFT2/Matlab/NFFT2_2D.m``,
-``NFFT/NFFT2/Matlab/NDFT2_2D.m`` and ``NFFT/NDFT2_2D.cu``) through ctypes.
+``NFFT/NFFT2/Matlab/NDFT2_2D.m`` and ``NFFT/NDFT2_2D.cu``, and of the
+Knab-window regridding ``BP_FBP_FFBP/knabNFFT2D.m`` with
+``NFFT_Based_Selvas_Approach_for_Signal_Interp_2D.m``, ``KnabWindow.m`` and
+``ConvWindow.m``) through ctypes.
 All coordinates here are in the reference's grid units (period N per
 dimension); callers with coordinates in [-0.5, 0.5) multiply by N first.
 
@@ -75,6 +78,10 @@ def _load():
         "oracle_ndft_type1": (None, [P, P, P, L, L, L, I, P]),
         "oracle_ndft2_2d_general": (None, [P, P, P, P, P, L, L, L, L, P]),
         "oracle_ndft2_2d_matlab": (None, [P, P, P, L, L, L, P]),
+        "oracle_conv_window": (D, [D, D, D]),
+        "oracle_conv_window_integral": (D, [D, D, D, D, D]),
+        "oracle_knab_window": (L, [D, D, I, L, P]),
+        "oracle_knab_nfft2d": (I, [D, D, P, L, P, L, P, P, P, L, L, D, D, I, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -221,3 +228,47 @@ def rel_l2(a, b) -> float:
     b = np.asarray(b, dtype=np.complex128).ravel()
     den = np.sqrt(np.sum(np.abs(b) ** 2))
     return float(np.sqrt(np.sum(np.abs(a - b) ** 2)) / den) if den > 0 else float(np.sqrt(np.sum(np.abs(a) ** 2)))
+
+
+def conv_window(f: float, B: float, T: float) -> float:
+    """Restated ConvWindow.m: the approximate prolate window of Selva's method."""
+    return _load().oracle_conv_window(float(f), float(B), float(T))
+
+
+def knab_window(T: float, B: float, P: int, N: int):
+    """Restated KnabWindow.m: returns (G, kg), G over frequencies -kg..kg."""
+    lib = _load()
+    kg = int(lib.oracle_knab_window(float(T), float(B), int(P), int(N), None))
+    if kg < 0:
+        return np.zeros(0), kg
+    G = np.zeros(2 * kg + 1)
+    lib.oracle_knab_window(float(T), float(B), int(P), int(N), _ptr(G))
+    return G, kg
+
+
+def knab_nfft2d(extrap, rho_in, cos_in, data, rho_out, cos_out, B1: float, B2: float, direct: bool = False):
+    """Restated knabNFFT2D.m (with Selva's NFFT interpolation).
+
+    rho_in: the Ncols input range samples (RHO_IN(1, :)); cos_in: the Nrows
+    input angle samples (COSALPHA_IN(:, 1)); data: Nrows x Ncols; rho_out,
+    cos_out: len1 x len2.  Returns (out len1 x len2, {"a", "b", "kgn", "kgm"}).
+    direct=True evaluates the same trigonometric sum exactly instead of by
+    NFFT1_2D."""
+    rho_in, cos_in = _f64(rho_in).ravel(), _f64(cos_in).ravel()
+    data = _c128(data)
+    rho_out, cos_out = _f64(rho_out), _f64(cos_out)
+    if rho_out.ndim != 2 or rho_out.shape != cos_out.shape:
+        raise ValueError("rho_out and cos_out must be equal-shape 2-D arrays")
+    Nrows, Ncols = data.shape
+    if rho_in.size != Ncols or cos_in.size != Nrows:
+        raise ValueError("axis lengths must match the data")
+    len1, len2 = rho_out.shape
+    out = np.zeros((len1, len2), dtype=np.complex128)
+    info = np.zeros(4, dtype=np.int64)
+    ev = complex(extrap)
+    rc = _load().oracle_knab_nfft2d(ev.real, ev.imag, _ptr(rho_in), Ncols, _ptr(cos_in), Nrows, _ptr(data),
+                                    _ptr(rho_out), _ptr(cos_out), len1, len2, float(B1), float(B2), int(bool(direct)),
+                                    _ptr(out), _ptr(info))
+    if rc != 0:
+        raise ValueError("oracle_knab_nfft2d: configuration the reference cannot run")
+    return out, dict(a=int(info[0]), b=int(info[1]), kgn=int(info[2]), kgm=int(info[3]))

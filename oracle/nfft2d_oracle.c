@@ -638,3 +638,212 @@ void oracle_ndft2_2d_matlab(const double *data, const double *x, const double *y
         for (long s = 0; s < M; ++s) o[r * M + s] = vec[r + N * s];
     free(vec);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Knab-window band-limited regridding (the SAR code's NFFT caller):         */
+/*   BP_FBP_FFBP/knabNFFT2D.m:1-79                                          */
+/*   BP_FBP_FFBP/NFFT_Based_Selvas_Approach_for_Signal_Interp_2D.m:4-28     */
+/*   BP_FBP_FFBP/KnabWindow.m:11-47, ConvWindow.m:5-11,                     */
+/*   IntervalIntersection.m:4-22                                            */
+/* ------------------------------------------------------------------------ */
+
+/* ConvWindow.m:5-11: W(f) = I0(pi B (T/2) sqrt(1 - (2f/B)^2)) / (B sinc(i B T/2))
+ * on |f| < B/2, else 0; MATLAB's sinc(i y) = sinh(pi y) / (pi y). */
+double oracle_conv_window(double f, double B, double T) {
+    if (!(fabs(f) < B / 2)) return 0.0;
+    const double q = 2.0 * f / B;
+    const double y = B * T / 2.0;
+    const double snc = (y == 0.0) ? 1.0 : sinh(OR_PI * y) / (OR_PI * y);
+    return oracle_bessel_i0(OR_PI * B * (T / 2.0) * sqrt(1.0 - q * q)) / (B * snc);
+}
+
+/* Adaptive Simpson quadrature with Richardson correction and tolerance
+ * halving on subdivision (Lyness 1969; the method of MATLAB's quad, which
+ * KnabWindow.m:40 calls with tolerance 1e-12). */
+static double simpson_step(double B1, double T, double a, double b, double fa, double fc, double fb, double tol,
+                           int depth) {
+    const double c = 0.5 * (a + b), h = b - a;
+    const double d = 0.5 * (a + c), e = 0.5 * (c + b);
+    const double fd = oracle_conv_window(d, B1, T), fe = oracle_conv_window(e, B1, T);
+    const double q1 = h / 6.0 * (fa + 4.0 * fc + fb);
+    const double q2 = h / 12.0 * (fa + 4.0 * fd + 2.0 * fc + 4.0 * fe + fb);
+    const double q = q2 + (q2 - q1) / 15.0;
+    if (depth >= 50 || fabs(q2 - q) <= tol || h <= 1e-300) return q;
+    return simpson_step(B1, T, a, c, fa, fd, fc, tol / 2, depth + 1) +
+           simpson_step(B1, T, c, b, fc, fe, fb, tol / 2, depth + 1);
+}
+
+double oracle_conv_window_integral(double lo, double hi, double B1, double T, double tol) {
+    if (!(hi > lo)) return 0.0;
+    /* three unequal starting panels keep the first estimate off symmetric
+     * cancellations */
+    const double h = 0.13579 * (hi - lo);
+    const double x[7] = {lo, lo + h, lo + 2 * h, 0.5 * (lo + hi), hi - 2 * h, hi - h, hi};
+    double y[7];
+    for (int i = 0; i < 7; ++i) y[i] = oracle_conv_window(x[i], B1, T);
+    return simpson_step(B1, T, x[0], x[2], y[0], y[1], y[2], tol, 0) +
+           simpson_step(B1, T, x[2], x[4], y[2], y[3], y[4], tol, 0) +
+           simpson_step(B1, T, x[4], x[6], y[4], y[5], y[6], tol, 0);
+}
+
+/* KnabWindow.m:11-47.  Returns kg; with G != NULL also fills G[0 .. 2kg]
+ * (frequencies -kg .. kg).  The operation order of kg and f(k) follows the
+ * MATLAB lines, since kg is a floor() of a quotient. */
+long oracle_knab_window(double T, double B, int P, long N, double *G) {
+    const double df = 1.0 / ((double)N * T);                       /* :16 */
+    const long kg = (long)floor((1.0 / T - B / 2.0) / df);          /* :19 */
+    if (!G || kg < 0) return kg;
+    const double B0 = 1.0 / T;                                      /* :24 */
+    const double B1 = B0 - B;                                       /* :25 */
+    const long n = 2 * kg + 1;
+    for (long i = 0; i < n; ++i) G[i] = 0.0;                        /* :29 */
+    long last = -1;
+    for (long k = 0; k <= kg; ++k) {
+        const double f = -df * (double)kg + df * (double)k;         /* :22 */
+        if (B1 / 2.0 <= f + B0 / 2.0)                               /* :26 */
+            G[k] = 1.0;                                             /* :32 */
+        else
+            last = k;
+    }
+    for (long k = 0; k <= last; ++k) {                              /* :36 */
+        const double f = -df * (double)kg + df * (double)k;
+        const double ia0 = -B1 / 2.0, ia1 = B1 / 2.0;               /* IntervalIntersection.m */
+        const double ib0 = f - B0 / 2.0, ib1 = f + B0 / 2.0;
+        if (ia1 < ib0 || ib1 < ia0) continue;                       /* :6-11 */
+        double lo, hi;
+        if (ib1 < ia1) {                                            /* :13-18 */
+            lo = ia0;
+            hi = ib1;
+        } else {                                                    /* :20 */
+            lo = ib0;
+            hi = ia1;
+        }
+        G[k] = oracle_conv_window_integral(lo, hi, B1, 2.0 * P * T, 1e-12);  /* :34,40 */
+    }
+    double *g2 = (double *)malloc(sizeof(double) * (size_t)n);
+    for (long i = 0; i < n; ++i) g2[i] = G[i] + G[n - 1 - i];      /* :45 */
+    g2[kg] -= 1.0;                                                  /* :46 */
+    for (long i = 0; i < n; ++i) G[i] = g2[i] / (double)N;          /* :47 */
+    free(g2);
+    return kg;
+}
+
+static double matlab_mean_diff(const double *v, long n) {
+    double s = 0.0;
+    for (long i = 0; i + 1 < n; ++i) s += v[i + 1] - v[i];
+    return s / (double)(n - 1);
+}
+
+/* knabNFFT2D.m:1-79 with the interpolation of
+ * NFFT_Based_Selvas_Approach_for_Signal_Interp_2D.m:4-28.
+ *
+ *   rho_in[Ncols], cos_in[Nrows]: the input raster's axes (RHO_IN(1,:),
+ *     COSALPHA_IN(:,1));
+ *   data: Nrows x Ncols complex, row <-> cos, column <-> rho (INPUT_DATA);
+ *   rho_out, cos_out: len1 x len2 (RHO_OUT, COSALPHA_OUT), row-major;
+ *   out: len1 x len2 complex.
+ *   info (may be NULL): {a, b, kgn, kgm}.
+ *   direct != 0 replaces the NFFT1_2D call by the exact direct sum of the
+ *   same trigonometric polynomial (to pin the NFFT's approximation).
+ * Returns 0, or -1 where the MATLAB code would fail (fewer than 2 x 2
+ * samples, an odd NFFT1_2D size, a spectrum wider than the padded grid). */
+int oracle_knab_nfft2d(double ev_re, double ev_im, const double *rho_in, long Ncols, const double *cos_in,
+                       long Nrows, const double *data, const double *rho_out, const double *cos_out, long len1,
+                       long len2, double B1, double B2, int direct, double *out, long *info) {
+    if (Nrows < 2 || Ncols < 2 || len1 < 1 || len2 < 1) return -1;  /* :15-20 */
+    const double T1 = matlab_mean_diff(rho_in, Ncols);               /* :6 */
+    const double T2 = matlab_mean_diff(cos_in, Nrows);               /* :7 */
+    const long Mo = len1 * len2;
+    /* :23-35 shifted outputs and their extent */
+    double mnr = INFINITY, mxr = -INFINITY, mnc = INFINITY, mxc = -INFINITY;
+    for (long p = 0; p < Mo; ++p) {
+        const double r = rho_out[p] - rho_in[0], c = cos_out[p] - cos_in[0];
+        if (r < mnr) mnr = r;
+        if (r > mxr) mxr = r;
+        if (c < mnc) mnc = c;
+        if (c > mxc) mxc = c;
+    }
+    double Nn = (mxr - mnr) / (T1 * (1.0 - 1.0 / (double)len2));     /* :34 */
+    double Mm = (mxc - mnc) / (T2 * (1.0 - 1.0 / (double)len1));     /* :35 */
+    if (Nn < 1 || isnan(Nn)) Nn = 1;                                 /* :37-42 */
+    if (Mm < 1 || isnan(Mm)) Mm = 1;
+    long a = (long)matlab_round((double)len2 / Nn);                  /* :45 */
+    long b = (long)matlab_round((double)len1 / Mm);                  /* :46 */
+    if (a < 2) a = 2;  /* :48-53; the zero-coordinate points appended there */
+    if (b < 2) b = 2;  /* :55-60   are cropped away again at :72            */
+    const int P = 18;                                                /* :63 */
+    const long kgn = oracle_knab_window(T1, B1, P, Ncols, NULL);     /* :64 */
+    const long kgm = oracle_knab_window(T2, B2, P, Nrows, NULL);     /* :65 */
+    if (info) {
+        info[0] = a;
+        info[1] = b;
+        info[2] = kgn;
+        info[3] = kgm;
+    }
+    const long NA = Ncols * a, MB = Nrows * b;  /* Interp_2D: N = Ncols, M = Nrows (INPUT_DATA.') */
+    if (kgn < 0 || kgm < 0 || (NA & 1) || (MB & 1) || NA / 2 - kgn - 1 < 0 || MB / 2 - kgm - 1 < 0) return -1;
+    double *Gn = (double *)malloc(sizeof(double) * (size_t)(2 * kgn + 1));
+    double *Gm = (double *)malloc(sizeof(double) * (size_t)(2 * kgm + 1));
+    oracle_knab_window(T1, B1, P, Ncols, Gn);
+    oracle_knab_window(T2, B2, P, Nrows, Gm);
+
+    /* Interp_2D:9  sF = fft2(INPUT_DATA.'): an Ncols x Nrows array */
+    cplx *sF = (cplx *)malloc(sizeof(cplx) * (size_t)(Ncols * Nrows));
+    const cplx *dc = (const cplx *)data;
+    for (long j = 0; j < Ncols; ++j)
+        for (long i = 0; i < Nrows; ++i) sF[j * Nrows + i] = dc[i * Ncols + j];
+    oracle_fft2d((double *)sF, Ncols, Nrows, -1);
+    /* Interp_2D:10-25: periodic repetition, window, (N a)(M b) factor, and
+     * the centered zero padding to NA x MB (even sizes: frequency k at
+     * index NA/2 + k) */
+    cplx *S = (cplx *)calloc((size_t)(NA * MB), sizeof(cplx));
+    const double scale = (double)NA * (double)MB;
+    for (long k1 = -kgn; k1 <= kgn; ++k1)
+        for (long k2 = -kgm; k2 <= kgm; ++k2) {
+            const cplx v = sF[pos_mod(k1, Ncols) * Nrows + pos_mod(k2, Nrows)];
+            const double g = Gn[k1 + kgn] * Gm[k2 + kgm] * scale;
+            S[(NA / 2 + k1) * MB + (MB / 2 + k2)].re = v.re * g;
+            S[(NA / 2 + k1) * MB + (MB / 2 + k2)].im = v.im * g;
+        }
+    /* Interp_2D:28  sUp = conj(NFFT1_2D(conj(S), rho_s/(T1/a), cos_s/(T2/b))) / (a b N M) */
+    double *x1 = (double *)malloc(sizeof(double) * (size_t)Mo);
+    double *x2 = (double *)malloc(sizeof(double) * (size_t)Mo);
+    for (long p = 0; p < Mo; ++p) {
+        x1[p] = (rho_out[p] - rho_in[0]) / (T1 / (double)a);
+        x2[p] = (cos_out[p] - cos_in[0]) / (T2 / (double)b);
+    }
+    for (long q = 0; q < NA * MB; ++q) S[q].im = -S[q].im;
+    cplx *o = (cplx *)out;
+    if (direct) {
+        oracle_ndft_type2((const double *)S, NA, MB, x1, x2, Mo, -1, out);
+    } else {
+        if (oracle_nfft1_2d((const double *)S, NA, MB, x1, x2, Mo, 2.0, 6, -1, out) != 0) {
+            free(Gn), free(Gm), free(sF), free(S), free(x1), free(x2);
+            return -1;
+        }
+    }
+    const double inv = 1.0 / ((double)a * (double)b * (double)Ncols * (double)Nrows);
+    for (long p = 0; p < Mo; ++p) {
+        o[p].re = o[p].re * inv;
+        o[p].im = -o[p].im * inv;
+    }
+    /* :75-78 extrapolation: columns whose RHO_OUT(1, :) and rows whose
+     * COSALPHA_OUT(:, 1) lie outside the input axes' range */
+    double rmin = INFINITY, rmax = -INFINITY, cmin = INFINITY, cmax = -INFINITY;
+    for (long j = 0; j < Ncols; ++j) {
+        if (rho_in[j] < rmin) rmin = rho_in[j];
+        if (rho_in[j] > rmax) rmax = rho_in[j];
+    }
+    for (long i = 0; i < Nrows; ++i) {
+        if (cos_in[i] < cmin) cmin = cos_in[i];
+        if (cos_in[i] > cmax) cmax = cos_in[i];
+    }
+    for (long j = 0; j < len2; ++j)
+        if (rho_out[j] < rmin || rho_out[j] > rmax)
+            for (long i = 0; i < len1; ++i) o[i * len2 + j].re = ev_re, o[i * len2 + j].im = ev_im;
+    for (long i = 0; i < len1; ++i)
+        if (cos_out[i * len2] < cmin || cos_out[i * len2] > cmax)
+            for (long j = 0; j < len2; ++j) o[i * len2 + j].re = ev_re, o[i * len2 + j].im = ev_im;
+    free(Gn), free(Gm), free(sF), free(S), free(x1), free(x2);
+    return 0;
+}

@@ -9,6 +9,11 @@ column-major meshgrid/reshape semantics kept literally):
   * ndft2_2d_m   -- NFFT/NFFT2/Matlab/NDFT2_2D.m:1-16
   * nfft2_2d_m   -- NFFT/NFFT2/Matlab/NFFT2_2D.m:1-72 (c = 2, K = 6)
   * nfft1_2d_m   -- BP_FBP_FFBP/NFFT1_2D.m:1-69       (c = 2, K = 6)
+  * knab_window_m  -- BP_FBP_FFBP/KnabWindow.m:11-47 with ConvWindow.m and
+                      IntervalIntersection.m (scipy's QUADPACK quad in place
+                      of MATLAB's adaptive Simpson quad, both at 1e-12)
+  * knab_nfft2d_m  -- BP_FBP_FFBP/knabNFFT2D.m:1-79 with
+                      NFFT_Based_Selvas_Approach_for_Signal_Interp_2D.m:4-28
 
 Cases:
   * "reftest": the reference's own acceptance test, Test_NFFT2_2D.m:5-29 --
@@ -17,14 +22,21 @@ Cases:
     NFFT2_2D(data, y, x, 22, 22); the MATLAB rand is replaced by a seeded PCG64.
   * "fwd":  NFFT1_2D on a 16 x 16 complex grid at 50 points.
   * "rect": NFFT2_2D with M1 = 16, M2 = 24 at 80 points.
+  * knab_golden.npz: knabNFFT2D on a 20 x 24 raster (rows: cos(alpha),
+    columns: rho) to a 14 x 33 output raster, rotated slightly so the
+    output points are not separable, with one column and one row outside
+    the input range (extrapolation value); and KnabWindow at (T, B, P, N) =
+    (0.25, 1.8, 18, 24).  B is chosen so that floor() in KnabWindow.m:19 and
+    round() in knabNFFT2D.m:45-46 are far from a tie.
 
-Run:  python tests/golden/make_golden.py   (writes the .npz next to this file)
+Run:  python tests/golden/make_golden.py   (writes the .npz files next to this file)
 """
 from __future__ import annotations
 
 import os
 
 import numpy as np
+from scipy.integrate import quad
 from scipy.special import i0
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -100,6 +112,130 @@ def nfft1_2d_m(data, x1, x2, c=2, K=6):
     return res
 
 
+def conv_window_m(f, B, T):
+    f = np.atleast_1d(np.asarray(f, dtype=np.float64))
+    W = np.zeros(f.shape)                                                     # ConvWindow.m:7
+    I = np.abs(f) < B / 2                                                     # :9
+    den = B * np.real(np.sinc(1j * B * T / 2))
+    W[I] = i0(np.pi * B * (T / 2) * np.sqrt(1 - (2 * f[I] / B) ** 2)) / den   # :11
+    return W
+
+
+def interval_intersection_m(IA, IB):
+    if IA[1] < IB[0] or IB[1] < IA[0]:                                        # IntervalIntersection.m:6
+        return None
+    if IB[1] < IA[1]:                                                         # :13
+        return [IA[0], IB[1]]
+    return [IB[0], IA[1]]                                                     # :20
+
+
+def knab_window_m(T, B, P, N):
+    df = 1 / (N * T)                                                          # KnabWindow.m:16
+    kg = int(np.floor((1 / T - B / 2) / df))                                  # :19
+    f = -df * kg + df * np.arange(0, kg + 1)                                  # :22
+    B0 = 1 / T                                                                # :24
+    B1 = B0 - B                                                               # :25
+    I = B1 / 2 <= (f + B0 / 2)                                                # :26
+    G = np.zeros(2 * kg + 1)                                                  # :29
+    G[:kg + 1][I] = 1                                                         # :32
+    notI = np.nonzero(~I)[0]
+    for k in range(notI[-1] + 1 if notI.size else 0):                        # :36
+        IInt = interval_intersection_m([-B1 / 2, B1 / 2], f[k] + np.array([-B0 / 2, B0 / 2]))
+        if IInt is not None:
+            G[k] = quad(lambda x: conv_window_m(x, B1, 2 * P * T)[0], IInt[0], IInt[1],
+                        epsabs=1e-12, epsrel=0, limit=500)[0]                 # :40
+    G = G + G[::-1]                                                           # :45
+    G[kg] -= 1                                                                # :46
+    return G / N, kg                                                          # :47
+
+
+def selva_interp_2d_m(INPUT_DATA, T1, T2, a, b, G, kgn, kgm, RHO_OUT_SHIFTED, COSALPHA_OUT_SHIFTED):
+    N, M = INPUT_DATA.shape                                                   # Interp_2D.m:6-7
+    sF = np.fft.fft2(INPUT_DATA)                                              # :9
+    sF = sF[np.ix_(np.mod(np.arange(-kgn, kgn + 1), N), np.mod(np.arange(-kgm, kgm + 1), M))]  # :10
+    sF = sF * G * (N * a) * (M * b)                                           # :11
+    csF = sF.shape[0]
+    if (b * M) % 2 == 0:                                                      # :14-18
+        sF = np.hstack([np.zeros((csF, M * b // 2 - kgm)), sF, np.zeros((csF, M * b // 2 - kgm - 1))])
+    else:
+        sF = np.hstack([np.zeros((csF, (M * b - 2 * kgm - 1) // 2)), sF, np.zeros((csF, (M * b - 2 * kgm - 1) // 2))])
+    rsF = sF.shape[1]
+    if (a * N) % 2 == 0:                                                      # :21-25
+        sF = np.vstack([np.zeros((N * a // 2 - kgn, rsF)), sF, np.zeros((N * a // 2 - kgn - 1, rsF))])
+    else:
+        sF = np.vstack([np.zeros(((N * a - 2 * kgn - 1) // 2, rsF)), sF, np.zeros(((N * a - 2 * kgn - 1) // 2, rsF))])
+    x1 = (RHO_OUT_SHIFTED / (T1 / a)).reshape(-1, order="F")                  # :28
+    x2 = (COSALPHA_OUT_SHIFTED / (T2 / b)).reshape(-1, order="F")
+    return (1 / (a * b * N * M)) * np.conj(nfft1_2d_m(np.conj(sF), x1, x2))
+
+
+def knab_nfft2d_m(ExtrapVal, RHO_IN, COSALPHA_IN, INPUT_DATA, RHO_OUT, COSALPHA_OUT, B1, B2):
+    T1 = np.mean(np.diff(RHO_IN[0, :]))                                       # knabNFFT2D.m:6
+    T2 = np.mean(np.diff(COSALPHA_IN[:, 0]))                                  # :7
+    RHO_OUT_SHIFTED = RHO_OUT - RHO_IN.flat[0]                                # :23
+    COSALPHA_OUT_SHIFTED = COSALPHA_OUT - COSALPHA_IN.flat[0]                 # :24
+    len1, len2 = RHO_OUT_SHIFTED.shape                                        # :26-27
+    N = (RHO_OUT_SHIFTED.max() - RHO_OUT_SHIFTED.min()) / (T1 * (1 - 1 / len2))           # :34
+    M = (COSALPHA_OUT_SHIFTED.max() - COSALPHA_OUT_SHIFTED.min()) / (T2 * (1 - 1 / len1))  # :35
+    if N < 1 or np.isnan(N):
+        N = 1
+    if M < 1 or np.isnan(M):
+        M = 1
+    a = int(matlab_round(len2 / N))                                           # :45
+    b = int(matlab_round(len1 / M))                                           # :46
+    if a < 2:                                                                 # :48-53
+        a = 2
+        ii = max(int(matlab_round(a * N)) - RHO_OUT_SHIFTED.shape[1], 0)
+        RHO_OUT_SHIFTED = np.hstack([RHO_OUT_SHIFTED, np.zeros((RHO_OUT_SHIFTED.shape[0], ii))])
+        COSALPHA_OUT_SHIFTED = np.hstack([COSALPHA_OUT_SHIFTED, np.zeros((COSALPHA_OUT_SHIFTED.shape[0], ii))])
+    if b < 2:                                                                 # :55-60
+        b = 2
+        ii = max(int(matlab_round(b * M)) - RHO_OUT_SHIFTED.shape[0], 0)
+        RHO_OUT_SHIFTED = np.vstack([RHO_OUT_SHIFTED, np.zeros((ii, RHO_OUT_SHIFTED.shape[1]))])
+        COSALPHA_OUT_SHIFTED = np.vstack([COSALPHA_OUT_SHIFTED, np.zeros((ii, COSALPHA_OUT_SHIFTED.shape[1]))])
+    P = 18                                                                    # :63
+    Gn, kgn = knab_window_m(T1, B1, P, INPUT_DATA.T.shape[0])                 # :64
+    Gm, kgm = knab_window_m(T2, B2, P, INPUT_DATA.T.shape[1])                 # :65
+    Y, X = np.meshgrid(Gm, Gn)                                                # :66
+    G = X * Y                                                                 # :67
+    res = selva_interp_2d_m(INPUT_DATA.T, T1, T2, a, b, G, kgn, kgm, RHO_OUT_SHIFTED, COSALPHA_OUT_SHIFTED)
+    result = res.reshape(RHO_OUT_SHIFTED.shape[0], COSALPHA_OUT_SHIFTED.shape[1], order="F")  # :71
+    result = result[:len1, :len2]                                             # :72
+    xout = (RHO_OUT[0, :] < RHO_IN[0, :].min()) | (RHO_OUT[0, :] > RHO_IN[0, :].max())              # :75
+    yout = (COSALPHA_OUT[:, 0] < COSALPHA_IN[:, 0].min()) | (COSALPHA_OUT[:, 0] > COSALPHA_IN[:, 0].max())
+    result[:, xout] = ExtrapVal                                               # :77
+    result[yout, :] = ExtrapVal                                               # :78
+    return result, dict(a=a, b=b, kgn=kgn, kgm=kgm)
+
+
+def knab_case(seed=20240602):
+    rng = np.random.default_rng(seed)
+    Nrows, Ncols = 20, 24
+    T1, T2 = 0.25, 0.02
+    rho_in = 50.0 + T1 * np.arange(Ncols)
+    cos_in = -0.2 + T2 * np.arange(Nrows)
+    RHO_IN, COSALPHA_IN = np.meshgrid(rho_in, cos_in)
+    data = rng.standard_normal((Nrows, Ncols)) + 1j * rng.standard_normal((Nrows, Ncols))
+    len1, len2 = 14, 33
+    r = np.linspace(rho_in[2], rho_in[-3], len2)
+    c = np.linspace(cos_in[2], cos_in[-3], len1)
+    Rg, Cg = np.meshgrid(r, c)
+    # slight rotation (in sample units) so the output points are not separable
+    u, v = (Rg - rho_in[0]) / T1, (Cg - cos_in[0]) / T2
+    th = 0.05
+    RHO_OUT = rho_in[0] + T1 * (np.cos(th) * u - np.sin(th) * v * 0.3)
+    COSALPHA_OUT = cos_in[0] + T2 * (np.sin(th) * u * 0.3 + np.cos(th) * v)
+    RHO_OUT[:, 0] = rho_in[0] - 0.4      # one column below the input range
+    COSALPHA_OUT[-1, :] = cos_in[-1] + 0.03  # one row above it
+    B1, B2 = 1.8, 17.0                   # 0.45 / T1 and 0.34 / T2
+    ev = 0.25 - 0.5j
+    out, info = knab_nfft2d_m(ev, RHO_IN, COSALPHA_IN, data, RHO_OUT, COSALPHA_OUT, B1, B2)
+    G, kg = knab_window_m(0.25, 1.8, 18, 24)
+    return dict(rho_in=rho_in, cos_in=cos_in, data=data, rho_out=RHO_OUT, cos_out=COSALPHA_OUT, B1=B1, B2=B2,
+                extrap=ev, out=out, a=info["a"], b=info["b"], kgn=info["kgn"], kgm=info["kgm"],
+                window_G=G, window_kg=kg)
+
+
 def main():
     rng = np.random.default_rng(20240601)
     out = {}
@@ -128,6 +264,10 @@ def main():
     path = os.path.join(HERE, "nfft_golden.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path}; reference-test NFFT vs NDFT error {float(out['reftest_err_pct']):.3e} %")
+    kpath = os.path.join(HERE, "knab_golden.npz")
+    kc = knab_case()
+    np.savez_compressed(kpath, **kc)
+    print(f"wrote {kpath}; a = {kc['a']}, b = {kc['b']}, kgn = {kc['kgn']}, kgm = {kc['kgm']}")
 
 
 if __name__ == "__main__":

@@ -24,6 +24,7 @@ workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -104,6 +105,31 @@ def least_squares_config5(seed: int = 4, N: int = 1024, M: int = 1 << 22, noise:
                                  "sigma": 2.0, "w": 6, "noise": noise, "seed": seed})
 
 
+def knab_regrid(seed: int = 5, N: int = 1024, L: int = 2048):
+    """Knab-window regridding (knabNFFT2D.m), the FFBP sub-image step: an
+    N x N raster on a (cos alpha, rho) grid -- range spacing 0.15, angle
+    spacing 1/N, bandwidths 0.5/T as FBP.m:95 passes them -- regridded to an
+    L x L output raster covering the input's interior, rotated slightly so
+    the output points are not separable."""
+    rng = np.random.default_rng(seed)
+    T1, T2 = 0.15, 1.0 / N
+    rho_in = 1000.0 + T1 * np.arange(N)
+    cos_in = -0.5 + T2 * np.arange(N)
+    m = 24  # stay P = 18 samples away from the raster's edges
+    r = np.linspace(rho_in[m], rho_in[-1 - m], L)
+    c = np.linspace(cos_in[m], cos_in[-1 - m], L)
+    Rg, Cg = np.meshgrid(r, c)
+    u, v = (Rg - rho_in[0]) / T1, (Cg - cos_in[0]) / T2
+    th = 0.01
+    rho_out = rho_in[0] + T1 * (np.cos(th) * u - np.sin(th) * v)
+    cos_out = cos_in[0] + T2 * (np.sin(th) * u + np.cos(th) * v)
+    data = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))).astype(np.complex64)
+    return dict(name=f"knab_{N}x{N}_to_{L}x{L}", rho_in=rho_in, cos_in=cos_in, rho_out=rho_out, cos_out=cos_out,
+                data=data, B1=0.5 / T1, B2=0.5 / T2,
+                config={"workload": "Knab-window regridding (knabNFFT2D)", "raster": [N, N], "outputs": [L, L],
+                        "P": 18, "sigma": 2.0, "w": 6, "bandwidth": "0.5/T", "seed": seed})
+
+
 def uneven_batch(seed: int = 3, count: int = 64):
     """64 transforms, N = 2^e with e ~ U{7..10} (square), M log-uniform in
     [1e4, 4e6], points uniform, coefficients N(0,1) complex; sigma 2, w 6."""
@@ -121,7 +147,7 @@ def uneven_batch(seed: int = 3, count: int = 64):
 
 
 WORKLOADS = {"polar": polar_raster, "config1": uniform_config1, "clustered": clustered_config3, "batch": uneven_batch,
-             "lsq": least_squares_config5}
+             "lsq": least_squares_config5, "knab": knab_regrid}
 
 
 # ---------------------------------------------------------------------------
@@ -612,6 +638,182 @@ def run_lsq(args, wl):
     plan.close()
 
 
+def knab_cpu_step(wl, rows):
+    import oracle
+    t0 = time.perf_counter()
+    oracle.knab_nfft2d(0.0, wl["rho_in"], wl["cos_in"], wl["data"], wl["rho_out"][:rows], wl["cos_out"][:rows],
+                       wl["B1"], wl["B2"])
+    return time.perf_counter() - t0
+
+
+def knab_cpu_baseline(wl, target_s: float = 15.0, steps: int | None = None):
+    """The oracle's restatement of knabNFFT2D on the first `rows` output rows
+    (the full raster FFT and NFFT grid; a block of whole rows keeps the
+    detected oversampling of the full output raster).  t(m) = a + b m from
+    two block sizes gives the rate for the full output raster."""
+    import oracle
+    oracle.build()
+    L1, L2 = wl["rho_out"].shape
+    rows = 8
+    dt = knab_cpu_step(wl, rows)
+    while rows < L1 and dt < 1.0:  # grow until the per-point work stands out of the fixed FFT cost
+        rows = min(L1, rows * 4)
+        dt = knab_cpu_step(wl, rows)
+    n = steps if steps is not None else max(1, min(20, int(target_s / max(dt, 1e-3))))
+    t = statistics.median([knab_cpu_step(wl, rows) for _ in range(n)])
+    M = L1 * L2
+    out = {"unit": UNIT, "cores": oracle.get_threads(), "kind": "port", "ms_per_step": t * 1e3,
+           "points": rows * L2, "sample_rate": rows * L2 / t}
+    if rows < L1:
+        r2 = max(1, rows // 4)
+        t2 = statistics.median([knab_cpu_step(wl, r2) for _ in range(max(3, n // 2))])
+        b = max((t - t2) / ((rows - r2) * L2), 0.0)
+        a = max(t - b * rows * L2, 0.0)
+        out["value"] = M / (a + b * M)
+        out["model"] = {"fixed_s": a, "per_point_s": b, "small_sample_points": r2 * L2, "small_sample_ms": t2 * 1e3}
+        how = f"the first {rows} and {r2} of {L1} output rows (x {L2})"
+    else:
+        out["value"] = M / t
+        how = f"all {L1} x {L2} outputs"
+    out["sample"] = (f"{how}, full {wl['data'].shape[0]}x{wl['data'].shape[1]} raster; median of {n} steps; "
+                     "oracle/nfft2d_oracle.c restating knabNFFT2D.m, KnabWindow.m and NFFT1_2D.m (OpenMP)")
+    return out
+
+
+def run_knab_reference(args, wl):
+    _, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cb = knab_cpu_baseline(wl, steps=max(1, args.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl["config"],
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_knab(args, wl):
+    """One step = one regridding of the raster onto the bound output raster:
+    raster FFT, windowed pad, oversampled FFT, halo fill, gather (the
+    extrapolation fill has nothing to do: every output is inside)."""
+    import torch
+
+    from miscellaneous_gb300 import knab
+    from miscellaneous_gb300._lib import Timings, load
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    L1, L2 = wl["rho_out"].shape
+    M = L1 * L2
+    rho_out = torch.from_numpy(wl["rho_out"]).to(dev)
+    cos_out = torch.from_numpy(wl["cos_out"]).to(dev)
+    data = torch.from_numpy(wl["data"]).to(dev)
+    r = knab.Regridder(wl["rho_in"], wl["cos_in"], wl["B1"], wl["B2"], precision="f32", stream=stream)
+    r.set_points(rho_out, cos_out)
+    out = torch.empty(L1, L2, dtype=torch.complex64, device=dev)
+    lib = load()
+    ph = r.plan_handle()
+    lib.nfft2d_enable_timing(ph, 1)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        r(data, 0.0, out=out)
+        flush.zero_()
+    torch.cuda.synchronize()
+    ms, stage = [], {"pad": 0.0, "fft": 0.0, "halo_fill": 0.0, "gather": 0.0}
+    tm = Timings()
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            ev0.record(stream)
+            r(data, 0.0, out=out)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+            lib.nfft2d_get_timings(ph, ctypes.byref(tm))
+            stage["pad"] += tm.pad_ms
+            stage["fft"] += tm.fft_type2_ms
+            stage["halo_fill"] += tm.halo_fill_ms
+            stage["gather"] += tm.gather_ms
+            flush.zero_()
+    t = sum(ms) / len(ms)
+    for k in stage:
+        stage[k] /= args.steps
+    stage["raster_fft_and_launch"] = max(t - sum(stage.values()), 0.0)
+    lib.nfft2d_enable_timing(ph, 0)
+    info = r.info()
+    G = info["N1"] * info["N2"] * 4  # sigma^2 N1 N2 oversampled cells
+    peak, peak_kind = measured_peaks()
+    alg = 20 * M + 8 * G
+    roofline = {"bound": "hbm", "kernel": "gather", "achieved": alg / (stage["gather"] * 1e-3) / 1e9, "peak": peak,
+                "unit": "GB/s", "frac": alg / (stage["gather"] * 1e-3) / 1e9 / peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "algorithmic_bytes_per_launch": alg,
+                "launch_ms": stage["gather"], "traffic": None}
+    # accuracy: the exact trigonometric sum of the same windowed spectrum
+    # (torch complex128 on the GPU) on 65,536 random outputs
+    accuracy = None
+    if not args.no_accuracy:
+        Gn, kgn = knab.KnabWindow(info["T1"], wl["B1"], 18, info["Ncols"])
+        Gm, kgm = knab.KnabWindow(info["T2"], wl["B2"], 18, info["Nrows"])
+        N1, N2 = info["N1"], info["N2"]
+        E = torch.fft.fft2(data.to(torch.complex128))
+        S = torch.zeros(N1, N2, dtype=torch.complex128, device=dev)
+        i1 = torch.arange(-kgm, kgm + 1, device=dev)
+        i2 = torch.arange(-kgn, kgn + 1, device=dev)
+        Ew = E[i1.remainder(info["Nrows"])][:, i2.remainder(info["Ncols"])]
+        S[N1 // 2 - kgm:N1 // 2 + kgm + 1, N2 // 2 - kgn:N2 // 2 + kgn + 1] = (
+            Ew * torch.from_numpy(Gm).to(dev)[:, None] * torch.from_numpy(Gn).to(dev)[None, :])
+        g = torch.Generator(device="cpu").manual_seed(7)
+        idx = torch.randperm(M, generator=g)[:65536].to(dev)
+        x1 = ((cos_out.reshape(-1) - wl["cos_in"][0]) / (info["Nrows"] * info["T2"]))
+        x2 = ((rho_out.reshape(-1) - wl["rho_in"][0]) / (info["Ncols"] * info["T1"]))
+        ref = ndft_type2_subset(S, x1, x2, idx, +1, torch)
+        accuracy = {"rel_l2": rel_l2(out.reshape(-1)[idx], ref, torch), "subset_points": 65536,
+                    "oracle": "exact sum of the Knab-windowed spectrum, torch complex128 on the GPU"}
+    e2e = None
+    if not args.no_e2e:
+        hd = torch.from_numpy(wl["data"]).pin_memory()
+        hout = torch.empty(L1, L2, dtype=torch.complex64).pin_memory()
+        hro = torch.from_numpy(wl["rho_out"]).pin_memory()
+        hco = torch.from_numpy(wl["cos_out"]).pin_memory()
+        dd = torch.empty_like(data)
+
+        def e2e_step():
+            rho_out.copy_(hro, non_blocking=True)
+            cos_out.copy_(hco, non_blocking=True)
+            dd.copy_(hd, non_blocking=True)
+            r.set_points(rho_out, cos_out)
+            r(dd, 0.0, out=out)
+            hout.copy_(out, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        es = []
+        for _ in range(args.steps):
+            ev0.record(stream)
+            e2e_step()
+            ev1.record(stream)
+            ev1.synchronize()
+            es.append(ev0.elapsed_time(ev1))
+        te = sum(es) / len(es)
+        e2e = {"value": M / (te * 1e-3), "unit": UNIT, "ms_per_step": te,
+               "h2d_bytes_per_step": hd.numel() * 8 + hro.numel() * 8 * 2, "d2h_bytes_per_step": hout.numel() * 8,
+               "includes": "H2D raster + output coordinates, set_points (extent, masks, binning), regrid, D2H"}
+    cpu = None if args.no_cpu_baseline else knab_cpu_baseline(wl)
+    line = {"metric": METRIC, "value": M / (t * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(wl["config"], l2="256 MB buffer written between timed steps", knab=info),
+            "stages_ms": stage, "roofline": roofline, "accuracy": accuracy, "e2e": e2e, "cpu_baseline": cpu,
+            "gpu_launches": 3 * args.steps,
+            "gpu_launches_note": "our kernels per step: knab pad, halo fill, gather (+ cuFFT x2, not counted), "
+                                 "extrapolation fill skipped (no masked lines)",
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+    r.close()
+
+
 def run_batch(args, wl):
     """Config 4: the batched graph launch vs one transform per launch (the
     library's own single-transform path with pre-created plans)."""
@@ -699,7 +901,12 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload](K=args.K) if (args.workload == "clustered" and args.K) else WORKLOADS[args.workload]()
-    if args.workload == "lsq":
+    if args.workload == "knab":
+        if args.impl == "reference":
+            run_knab_reference(args, wl)
+        else:
+            run_knab(args, wl)
+    elif args.workload == "lsq":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the least-squares workload has no reference counterpart"}))
             return

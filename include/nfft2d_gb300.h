@@ -227,6 +227,66 @@ int nfft2d_batch_synchronize(nfft2d_batch batch);
 int nfft2d_forward_small_noalloc(int N1, int N2, int K, long long M, const float *x1, const float *x2, int units,
                                  const void *F, void *f, void *stream);
 
+/* ---- Knab-window band-limited regridding ---------------------------------
+ * Replaces BP_FBP_FFBP/knabNFFT2D.m:1-79 (with
+ * NFFT_Based_Selvas_Approach_for_Signal_Interp_2D.m:4-28, KnabWindow.m:11-47,
+ * ConvWindow.m:5-11), the SAR back-projection code's caller of the forward
+ * NFFT.  A raster sampled on a rectilinear grid is interpolated to arbitrary
+ * output points as a band-limited trigonometric polynomial:
+ *
+ *   data     Nrows x Ncols complex (float2 / double2 by precision), row-major,
+ *            DEVICE; row i sits at cos_in[i], column j at rho_in[j]
+ *            (INPUT_DATA with COSALPHA_IN(:,1) and RHO_IN(1,:));
+ *   rho_in   Ncols reals, cos_in  Nrows reals: the raster axes, HOST arrays;
+ *            T1 = mean(diff(rho_in)), T2 = mean(diff(cos_in));
+ *   B1, B2   bilateral bandwidths of the signal along rho and cos alpha
+ *            (0 < B < 1/T);
+ *   rho_out, cos_out  len1 x len2 output coordinates, row-major, DEVICE;
+ *   out      len1 x len2 complex, DEVICE.
+ *
+ * As in the reference: the Knab windows use P = 18; the oversampling factors
+ * a, b >= 2 are detected from the output points' extent (knabNFFT2D.m:34-60);
+ * the interpolation is a type-2 NFFT with sign +1 (sigma = 2, K = 6) on the
+ * (b Nrows) x (a Ncols) zero-padded windowed spectrum; output columns whose
+ * rho_out[0][j] and rows whose cos_out[i][0] lie outside the input axes get
+ * the extrapolation value (:75-78).  Returns NFFT2D_ERR_INVALID_ARG where
+ * the reference's NFFT1_2D cannot run (odd b Nrows or a Ncols). */
+typedef struct nfft2d_knab_s *nfft2d_knab;
+
+typedef struct {
+    int Nrows, Ncols;      /* raster                                              */
+    int kgn, kgm;          /* window half-lengths along rho / cos alpha           */
+    double T1, T2;         /* mean input spacings                                 */
+    int a, b;              /* detected oversampling (0 before set_points)         */
+    int N1, N2;            /* internal NFFT grid: b*Nrows x a*Ncols               */
+    int len1, len2;        /* output raster                                       */
+    int masked_lines;      /* output rows + columns set to the extrapolation value */
+} nfft2d_knab_info;
+
+/* Host only (no GPU): the Knab window of KnabWindow.m, G[0 .. 2kg] over
+ * frequencies -kg .. kg.  With G = NULL only *kg is returned; otherwise
+ * G_len must be >= 2*kg + 1. */
+int nfft2d_knab_window(double T, double B, int P, int N, double *G, int G_len, int *kg);
+
+int nfft2d_knab_create(nfft2d_knab *knab, int Nrows, int Ncols, const double *rho_in, const double *cos_in,
+                       double B1, double B2, int precision, void *stream);
+int nfft2d_knab_destroy(nfft2d_knab knab);
+/* Bind the output points (FP32 or FP64 coordinates); synchronizes. */
+int nfft2d_knab_set_points(nfft2d_knab knab, int len1, int len2, const void *rho_out, const void *cos_out,
+                           int coord_dtype);
+/* Asynchronous on the stream given at creation. */
+int nfft2d_knab_execute(nfft2d_knab knab, double extrap_re, double extrap_im, const void *data, void *out);
+int nfft2d_knab_get_info(nfft2d_knab knab, nfft2d_knab_info *info);
+int nfft2d_knab_synchronize(nfft2d_knab knab);
+/* The internal NFFT plan (for nfft2d_enable_timing / nfft2d_get_timings);
+ * NULL before set_points.  Owned by the regridder. */
+nfft2d_plan nfft2d_knab_plan(nfft2d_knab knab);
+/* The whole knabNFFT2D call: create, set_points (FP64 coordinates), execute,
+ * synchronize, destroy. */
+int nfft2d_knab_nfft2d(double extrap_re, double extrap_im, const double *rho_in, int Ncols, const double *cos_in,
+                       int Nrows, const void *data, const double *rho_out, const double *cos_out, int len1, int len2,
+                       double B1, double B2, int precision, void *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,12 +7,12 @@ with ctypes and uses PyTorch only for device memory and streams.
 """
 from ._lib import NFFT2DError, LIB_PATH, load  # noqa: F401
 
-__all__ = ["NFFT2DError", "LIB_PATH", "load", "nfft"]
+__all__ = ["NFFT2DError", "LIB_PATH", "load", "nfft", "knab", "shard", "autotune"]
 
 
 def __getattr__(name):
     # torch is imported lazily so the C-ABI checks run without it.
-    if name in ("nfft", "shard"):
+    if name in ("nfft", "shard", "knab", "autotune"):
         import importlib
         return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)

@@ -65,6 +65,16 @@ class Timings(ctypes.Structure):
         return {name: float(getattr(self, name)) for name, _ in self._fields_}
 
 
+class KnabInfo(ctypes.Structure):
+    _fields_ = [("Nrows", ctypes.c_int), ("Ncols", ctypes.c_int), ("kgn", ctypes.c_int), ("kgm", ctypes.c_int),
+                ("T1", ctypes.c_double), ("T2", ctypes.c_double), ("a", ctypes.c_int), ("b", ctypes.c_int),
+                ("N1", ctypes.c_int), ("N2", ctypes.c_int), ("len1", ctypes.c_int), ("len2", ctypes.c_int),
+                ("masked_lines", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class NFFT2DError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
@@ -107,6 +117,15 @@ _SIGNATURES = {
     "nfft2d_batch_adjoint": (_I, [_P, _P, _P]),
     "nfft2d_batch_set_graph": (_I, [_P, _I]),
     "nfft2d_batch_synchronize": (_I, [_P]),
+    "nfft2d_knab_window": (_I, [_D, _D, _I, _I, _P, _I, ctypes.POINTER(_I)]),
+    "nfft2d_knab_create": (_I, [ctypes.POINTER(_P), _I, _I, _P, _P, _D, _D, _I, _P]),
+    "nfft2d_knab_destroy": (_I, [_P]),
+    "nfft2d_knab_set_points": (_I, [_P, _I, _I, _P, _P, _I]),
+    "nfft2d_knab_execute": (_I, [_P, _D, _D, _P, _P]),
+    "nfft2d_knab_get_info": (_I, [_P, ctypes.POINTER(KnabInfo)]),
+    "nfft2d_knab_synchronize": (_I, [_P]),
+    "nfft2d_knab_plan": (_P, [_P]),
+    "nfft2d_knab_nfft2d": (_I, [_D, _D, _P, _I, _P, _I, _P, _P, _P, _I, _I, _D, _D, _I, _P, _P]),
 }
 
 

@@ -143,4 +143,20 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
 void release_plan(nfft2d_plan_s *p);
 int tensor_map_for(nfft2d_plan_s *p);
 
+// Bin points whose grid-unit coordinates are (x - o) * u per dimension (the
+// public set_points uses o = 0 and u from its units argument).
+int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype, double u1,
+                      double u2, double o1, double o2);
+
+// A type-2 transform whose deapodized, zero-padded coefficients are written
+// into the grid interior by `pad` (launched on the plan's stream, timed as
+// the pad stage) instead of by the plan's own pad kernel; then FFT, halo
+// fill and gather as nfft2d_type2.
+typedef cudaError_t (*PadFn)(const nfft2d_plan_s *p, const void *ctx);
+int type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const void *ctx);
+
+// Host FP64 helpers shared by the plan and the Knab regridder.
+double bessel_i0_host(double x);
+void deapod_table_host(int N, int n, int K, double alpha, double *out);
+
 }  // namespace nfft2d

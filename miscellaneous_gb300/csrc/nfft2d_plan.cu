@@ -22,16 +22,8 @@
 
 using namespace nfft2d;
 
-namespace {
-
-constexpr double kPi = 3.141592653589793238462643383279502884;
-
-// ---------------------------------------------------------------------------
-// host math (plan time, FP64)
-// ---------------------------------------------------------------------------
-
 // I0 by its power series (Abramowitz & Stegun 9.6.12); all terms positive.
-double host_bessel_i0(double x) {
+double nfft2d::bessel_i0_host(double x) {
     const double q = 0.25 * x * x;
     double term = 1.0, sum = 1.0;
     for (int j = 1; j < 500; ++j) {
@@ -41,6 +33,27 @@ double host_bessel_i0(double x) {
     }
     return sum;
 }
+
+// S / phi(xi_k) for k = i - N/2, i < N: S = sinh(alpha K)/(pi K) (the window
+// normalisation), phi(xi) = I0(K sqrt(alpha^2 - xi^2)), xi_k = 2 pi k / n
+// (NFFT1_2D.m:17-22, NFFT2_2D.cu:60-69).
+void nfft2d::deapod_table_host(int N, int n, int K, double alpha, double *out) {
+    const double pi = 3.141592653589793238462643383279502884;
+    const double S = std::sinh(alpha * K) / (pi * K);
+    for (int i = 0; i < N; ++i) {
+        const double xi = 2.0 * pi * (i - N / 2) / n;
+        out[i] = S / bessel_i0_host(K * std::sqrt(alpha * alpha - xi * xi));
+    }
+}
+
+namespace {
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// ---------------------------------------------------------------------------
+// host math (plan time, FP64)
+// ---------------------------------------------------------------------------
+
 
 int status_from_cuda(cudaError_t e) {
     if (e == cudaSuccess) return NFFT2D_OK;
@@ -265,13 +278,15 @@ __device__ __forceinline__ int wrap_index(long long m, int n) {
     return static_cast<int>(r < 0 ? r + n : r);
 }
 
-// Reduction of one coordinate: v = x * s (s = sigma * unit scale), mu = rint(v)
-// wrapped into [0, n), t = v - mu in [-1/2, 1/2] (NFFT2_2D.cu:167-173 does the
-// same in the data precision).  FP32 coordinates with a power-of-two scale take
+// Reduction of one coordinate: v = (x - o) * s (s = sigma * unit scale, o an
+// origin, 0 for the plain transforms), mu = rint(v) wrapped into [0, n),
+// t = v - mu in [-1/2, 1/2] (NFFT2_2D.cu:167-173 does the same in the data
+// precision).  FP32 coordinates with a power-of-two scale and no origin take
 // an exact FP32 path (the product, rint and the difference are all exact);
 // everything else is reduced in FP64.
 template <typename CT, typename TT>
-__device__ __forceinline__ bool reduce_coord(CT x, double s, float sf, bool exact_f32, int n, int &mu, TT &t) {
+__device__ __forceinline__ bool reduce_coord(CT x, double o, double s, float sf, bool exact_f32, int n, int &mu,
+                                             TT &t) {
     if (exact_f32) {
         const float v = static_cast<float>(x) * sf;
         if (isfinite(v) && fabsf(v) < 1073741824.0f) {
@@ -282,7 +297,7 @@ __device__ __forceinline__ bool reduce_coord(CT x, double s, float sf, bool exac
         }
         if (!isfinite(v)) return false;
     }
-    double v = static_cast<double>(x) * s;
+    double v = (static_cast<double>(x) - o) * s;
     if (!isfinite(v)) return false;
     if (fabs(v) >= 1073741824.0) v -= static_cast<double>(n) * floor(v / n);  // keep the integer part in range
     const double m = rint(v);
@@ -292,16 +307,16 @@ __device__ __forceinline__ bool reduce_coord(CT x, double s, float sf, bool exac
 }
 
 template <typename CT, typename RecT>
-__global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double s1, double s2,
-                            float s1f, float s2f, int exact_f32, Geom g, RecT *__restrict__ tmp,
+__global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double o1, double o2,
+                            double s1, double s2, float s1f, float s2f, int exact_f32, Geom g, RecT *__restrict__ tmp,
                             unsigned *__restrict__ ranks, unsigned *__restrict__ cell_count,
                             int *__restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
     RecT r;
     int mu1, mu2;
-    const bool ok1 = reduce_coord(x1[i], s1, s1f, exact_f32 != 0, g.n1, mu1, r.t1);
-    const bool ok2 = reduce_coord(x2[i], s2, s2f, exact_f32 != 0, g.n2, mu2, r.t2);
+    const bool ok1 = reduce_coord(x1[i], o1, s1, s1f, exact_f32 != 0, g.n1, mu1, r.t1);
+    const bool ok2 = reduce_coord(x2[i], o2, s2, s2f, exact_f32 != 0, g.n2, mu2, r.t2);
     if (!ok1 || !ok2) {
         latch_error(status, kErrNonfinite);
         tmp[i].orig = static_cast<int>(kInvalidKey);
@@ -808,15 +823,10 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     // Deapodization tables S / phi(xi_k), S = sinh(alpha K)/(pi K) (the
     // window normalisation), phi(xi) = I0(K sqrt(alpha^2 - xi^2)),
     // xi_k = 2 pi k / (sigma N)  (NFFT1_2D.m:17-22, NFFT2_2D.cu:60-69).
-    const double S = std::sinh(alpha * K) / (kPi * K);
     for (int d = 0; d < 2; ++d) {
         const int N = d == 0 ? N1 : N2;
-        const double n = d == 0 ? g.n1 : g.n2;
         std::vector<double> tab(N);
-        for (int i = 0; i < N; ++i) {
-            const double xi = 2.0 * kPi * (i - N / 2) / n;
-            tab[i] = S / host_bessel_i0(K * std::sqrt(alpha * alpha - xi * xi));
-        }
+        deapod_table_host(N, d == 0 ? g.n1 : g.n2, K, alpha, tab.data());
         void *dst = d == 0 ? p->deap1 : p->deap2;
         if (precision == NFFT2D_F64) {
             e = cudaMemcpy(dst, tab.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
@@ -925,9 +935,27 @@ int nfft2d_get_info(nfft2d_plan p, nfft2d_info *info) {
 
 static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
+    if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
+        return NFFT2D_ERR_INVALID_ARG;
+    double u1 = 1.0, u2 = 1.0;
+    if (units == NFFT2D_UNITS_UNIT) {
+        u1 = p->N1;
+        u2 = p->N2;
+    } else if (units == NFFT2D_UNITS_RADIANS) {
+        u1 = p->N1 / (2.0 * kPi);
+        u2 = p->N2 / (2.0 * kPi);
+    }
+    return nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0);
+}
+
+extern "C++" {
+int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype,
+                              double u1, double u2, double o1, double o2) {
+    if (!p) return NFFT2D_ERR_INVALID_ARG;
     if (M < 0 || M > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;
     if (coord_dtype != NFFT2D_COORD_F32 && coord_dtype != NFFT2D_COORD_F64) return NFFT2D_ERR_INVALID_ARG;
-    if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
+    if (!(u1 > 0) || !(u2 > 0) || !std::isfinite(u1) || !std::isfinite(u2) || !std::isfinite(o1) ||
+        !std::isfinite(o2))
         return NFFT2D_ERR_INVALID_ARG;
     if (M > 0 && (!x1 || !x2)) return NFFT2D_ERR_INVALID_ARG;
     p->points_valid = false;
@@ -942,21 +970,13 @@ static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, co
         return NFFT2D_OK;
     }
     const Geom &g = p->g;
-    double u1 = 1.0, u2 = 1.0;
-    if (units == NFFT2D_UNITS_UNIT) {
-        u1 = p->N1;
-        u2 = p->N2;
-    } else if (units == NFFT2D_UNITS_RADIANS) {
-        u1 = p->N1 / (2.0 * kPi);
-        u2 = p->N2 / (2.0 * kPi);
-    }
     const double s1 = p->sigma * u1, s2 = p->sigma * u2;
     p->xscale1 = s1;
     p->xscale2 = s2;
     // exact FP32 reduction when both scales are powers of two and x is FP32
     int e1 = 0, e2 = 0;
     const bool pow2 = std::frexp(s1, &e1) == 0.5 && std::frexp(s2, &e2) == 0.5;
-    const int exact = (coord_dtype == NFFT2D_COORD_F32 && pow2) ? 1 : 0;
+    const int exact = (coord_dtype == NFFT2D_COORD_F32 && pow2 && o1 == 0.0 && o2 == 0.0) ? 1 : 0;
     const float s1f = static_cast<float>(s1), s2f = static_cast<float>(s2);
     stage_begin(p, ST_SORT);
     NFFT_TRY_CUDA(cudaMemsetAsync(p->d_status, 0, 4 * sizeof(int), p->stream));
@@ -966,20 +986,20 @@ static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, co
     if (p->precision == NFFT2D_F64) {
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec64><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, s1, s2, s1f, s2f, exact, g,
+                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
                 static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
         else
             k_bin_pass1<float, Rec64><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, s1, s2, s1f, s2f, exact, g,
+                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
                 static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
     } else {
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec32><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, s1, s2, s1f, s2f, exact, g,
+                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
                 static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
         else
             k_bin_pass1<float, Rec32><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, s1, s2, s1f, s2f, exact, g,
+                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
                 static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
     }
     NFFT_TRY_CUDA(cudaGetLastError());
@@ -1011,6 +1031,31 @@ static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, co
     p->points_valid = true;
     return NFFT2D_OK;
 }
+}  // extern "C++"
+
+extern "C++" {
+int nfft2d::type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const void *ctx) {
+    if (!p || !pad) return NFFT2D_ERR_INVALID_ARG;
+    if (sign != 1 && sign != -1) return NFFT2D_ERR_INVALID_ARG;
+    if (!p->points_valid) return NFFT2D_ERR_NO_POINTS;
+    timer_reset(p, CALL_TYPE2);
+    if (p->M == 0) return NFFT2D_OK;
+    stage_begin(p, ST_PAD);
+    NFFT_TRY_CUDA(pad(p, ctx));
+    stage_end(p, ST_PAD);
+    stage_begin(p, ST_FFT2);
+    int st = run_fft(p, sign);
+    if (st != NFFT2D_OK) return st;
+    stage_end(p, ST_FFT2);
+    stage_begin(p, ST_FILL);
+    NFFT_TRY_CUDA(launch_halo_fill(p));
+    stage_end(p, ST_FILL);
+    stage_begin(p, ST_GATHER);
+    NFFT_TRY_CUDA(launch_gather(p, f));
+    stage_end(p, ST_GATHER);
+    return NFFT2D_OK;
+}
+}  // extern "C++"
 
 static int nfft2d_type2_impl(nfft2d_plan p, int sign, const void *F, void *f) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;

@@ -137,3 +137,25 @@ def test_package_fails_loudly_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.load()
+
+
+@pytest.mark.parametrize("T,B,N", [(0.25, 1.8, 24), (0.1, 4.5, 64), (0.3, 0.5 / 0.3, 160), (1.0, 0.5, 512)])
+def test_knab_window_host_matches_oracle(lib, orc, T, B, N):
+    # nfft2d_knab_window is host FP64 (Gauss-Legendre in theta), the oracle
+    # restates MATLAB's adaptive Simpson quad at 1e-12: equal kg, G within
+    # the oracle's quadrature tolerance
+    from miscellaneous_gb300 import knab
+    G, kg = knab.KnabWindow(T, B, 18, N)
+    Go, kgo = orc.knab_window(T, B, 18, N)
+    assert kg == kgo
+    assert abs(G - Go).max() * N < 2e-12
+
+
+def test_knab_window_rejects_bad_parameters(lib):
+    kg = ctypes.c_int()
+    for T, B, N in [(0.0, 1.0, 16), (0.5, 0.0, 16), (0.5, 2.5, 16), (0.5, 1.0, 0)]:
+        assert lib.nfft2d_knab_window(T, B, 18, N, None, 0, ctypes.byref(kg)) == _lib.ERR_INVALID_ARG
+    assert lib.nfft2d_knab_window(0.5, 1.0, 18, 16, None, 0, ctypes.byref(kg)) == 0
+    G = (ctypes.c_double * 3)()
+    # a buffer shorter than 2 kg + 1 is refused
+    assert lib.nfft2d_knab_window(0.5, 1.0, 18, 16, G, 3, ctypes.byref(kg)) == _lib.ERR_INVALID_ARG

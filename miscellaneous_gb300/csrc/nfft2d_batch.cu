@@ -203,7 +203,7 @@ __device__ __forceinline__ void batch_issue(const BatchDesc *__restrict__ d, int
 template <int K, bool COMP>
 __global__ void __launch_bounds__(kThreads, 4)
     k_batch_gather(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total, Geom g0,
-                   float alpha, float cn, float kp, int *status) {
+                   const __grid_constant__ WinPoly wp, int *status) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_ok;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                 continue;
             }
             out[raw.w] = gather_point<K, COMP>(patch, g0.PC, g0.Ke, lr, lc, __int_as_float(raw.x),
-                                               __int_as_float(raw.y), alpha, cn, kp);
+                                               __int_as_float(raw.y), wp);
         }
         __syncthreads();
     }
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, 4)
 template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32)
     k_batch_spread(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total, Geom g0,
-                   float alpha, float cn, float kp, int chunk, int *work, int *status) {
+                   const __grid_constant__ WinPoly wp, int chunk, int *work, int *status) {
     extern __shared__ unsigned char smem_raw[];
     constexpr int PR = kRegTile + 2 * K;
     constexpr int SP = point_scratch<K>();
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
         float2 acc[PR];
 #pragma unroll
         for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
-        spread_points<K>(D.recs, ch.y, ch.z, r0, c0, io[t].in, scr, acc, alpha, cn, kp, status);
+        spread_points<K>(D.recs, ch.y, ch.z, r0, c0, io[t].in, scr, acc, wp, status);
         flush_patch<K>(&D.tmap, patch, acc, g0.H, r0, c0, pending);
         pending = true;
     }
@@ -337,7 +337,7 @@ struct nfft2d_batch_s {
     cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_io = nullptr;
     bool io_pending = false;
     Geom g0{};
-    float alpha = 0, cn = 0, kp = 0;
+    WinPoly poly{};  // window polynomials (shared sigma, K)
 };
 
 namespace {
@@ -411,8 +411,8 @@ int enqueue_stages(nfft2d_batch_s *b, int type) {
             if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
             B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem));
             const int blocks = std::max(1, std::min(b->total_chunks, std::max(per_sm, 1) * sms));
-            kernel<<<blocks, kThreads, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0, b->alpha, b->cn,
-                                                          b->kp, b->d_status);
+            kernel<<<blocks, kThreads, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0, b->poly,
+                                                          b->d_status);
             B_TRY(cudaGetLastError());
         }
     } else {
@@ -428,8 +428,8 @@ int enqueue_stages(nfft2d_batch_s *b, int type) {
             const int blocks = static_cast<int>(std::max(1LL, std::min<long long>((items + kSpreadWarps - 1) / kSpreadWarps,
                                                                             std::max(per_sm, 1) * sms)));
             B_TRY(cudaMemsetAsync(b->d_work, 0, sizeof(int), b->stream));
-            kernel<<<blocks, kSpreadWarps * 32, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0, b->alpha,
-                                                                   b->cn, b->kp, chunk, b->d_work, b->d_status);
+            kernel<<<blocks, kSpreadWarps * 32, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0,
+                                                                   b->poly, chunk, b->d_work, b->d_status);
             B_TRY(cudaGetLastError());
         }
         k_batch_fold<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
@@ -574,9 +574,7 @@ int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *
     if (cudaMalloc(&b->d_status, 4 * sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMemsetAsync(b->d_status, 0, 4 * sizeof(int), b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     b->g0 = b->plans[0]->g;
-    b->alpha = static_cast<float>(b->plans[0]->w.alpha);
-    b->cn = static_cast<float>(b->plans[0]->w.cn);
-    b->kp = static_cast<float>(b->plans[0]->w.kp);
+    b->poly = b->plans[0]->poly;
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     *out = b;
     return NFFT2D_OK;

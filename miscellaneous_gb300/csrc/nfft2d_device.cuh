@@ -139,6 +139,20 @@ __device__ __forceinline__ void weights_f32(float t, float (&w)[2 * K + 1], floa
     }
 }
 
+// All 2K+1 taps from the plan's polynomials: Horner steps on FP32 FMAs whose
+// coefficients are read from kernel parameter space (uniform across the warp).
+template <int K>
+__device__ __forceinline__ void weights_poly(float t, float (&w)[2 * K + 1], const WinPoly &P) {
+    constexpr int D = poly_degree(K);
+#pragma unroll
+    for (int a = 0; a <= 2 * K; ++a) w[a] = P.c[D][a];
+#pragma unroll
+    for (int d = D - 1; d >= 0; --d) {
+#pragma unroll
+        for (int a = 0; a <= 2 * K; ++a) w[a] = fmaf(w[a], t, P.c[d][a]);
+    }
+}
+
 // Derivative dw/dt of the same taps (d/dt of w(t - m)).
 //   interior: dw/du = w * (alpha s coth(alpha s) - 1) * (-u) / s^2
 //   edge:     dw/du = cn * g'(P) * (-2u),  g(P) = sinh(alpha sqrt(P))/sqrt(P),

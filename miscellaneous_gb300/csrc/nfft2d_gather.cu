@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                                                            const Rec32 *__restrict__ recs,
                                                            const int4 *__restrict__ chunks, float2 *__restrict__ out,
                                                            const float2 *__restrict__ vin, float *__restrict__ g1,
-                                                           float *__restrict__ g2, const KArgs a) {
+                                                           float *__restrict__ g2,
+                                                           const __grid_constant__ KArgs a) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_ok;
@@ -107,11 +108,11 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                 continue;
             }
             if (MODE == 0) {
-                out[raw.w] = gather_point<K, COMP>(patch, PC, g.Ke, lr, lc, t1, t2, a.alpha, a.cn, a.kp);
+                out[raw.w] = gather_point<K, COMP>(patch, PC, g.Ke, lr, lc, t1, t2, a.poly);
             } else {
                 float w1[W], w2[W], d1[W], d2[W];
-                weights_f32<K>(t1, w1, a.alpha, a.cn, a.kp);
-                weights_f32<K>(t2, w2, a.alpha, a.cn, a.kp);
+                weights_poly<K>(t1, w1, a.poly);
+                weights_poly<K>(t2, w2, a.poly);
                 const float2 *base = patch + lr * PC + lc + (g.Ke - K);
                 dweights_f32<K>(t1, w1, d1, a.alpha, a.cn);
                 dweights_f32<K>(t2, w2, d2, a.alpha, a.cn);
@@ -156,7 +157,7 @@ struct CxOf<double> {
 template <int K, typename Real>
 __device__ __forceinline__ void weights_any(Real t, Real (&w)[2 * K + 1], const KArgs &a) {
     if constexpr (sizeof(Real) == 4)
-        weights_f32<K>(t, w, a.alpha, a.cn, a.kp);
+        weights_poly<K>(t, w, a.poly);
     else
         weights_f64<K>(t, w, a.alpha_d, a.cn_d);
 }
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
                                                             typename CxOf<Real>::type *__restrict__ out,
                                                             const typename CxOf<Real>::type *__restrict__ vin,
                                                             Real *__restrict__ g1, Real *__restrict__ g2,
-                                                            const KArgs a) {
+                                                            const __grid_constant__ KArgs a) {
     using Cx = typename CxOf<Real>::type;
     constexpr int W = 2 * K + 1;
     const int i = blockIdx.x * kThreads + threadIdx.x;

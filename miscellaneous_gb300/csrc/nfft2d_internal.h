@@ -35,6 +35,23 @@ struct __align__(8) Rec64 {
     int orig;
 };
 
+// The FP32 window as polynomials: tap a (grid offset m = a - K) of a point
+// with fractional offset t in [-1/2, 1/2] is w(t - m) = sum_d c[d][a] t^d,
+// degree kPolyDegree(K); fitted in FP64 at plan time (Chebyshev nodes), max
+// error < 1e-9 against the closed form for every sigma >= 1.25, 2 <= K <= 8.
+// The kernels evaluate all taps by Horner steps on FP32 FMAs, no special
+// functions (piecewise-polynomial kernel evaluation, as published for
+// FINUFFT by Barnett, Magland and af Klinteberg, SIAM J. Sci. Comput. 2019).
+constexpr int kPolyCoef = 11;
+__host__ __device__ constexpr int poly_degree(int K) { return K <= 3 ? 10 : 9; }
+struct WinPoly {
+    float c[kPolyCoef][2 * kMaxK + 1];
+};
+
+// Fit the polynomials of the window for (sigma, K); returns the max abs
+// error of the FP64 fit on a dense grid (negative on invalid arguments).
+double fit_window_poly(double sigma, int K, WinPoly *out);
+
 // Window constants of one plan (both precisions are filled).
 struct WinConst {
     double alpha;   // (2 - 1/sigma) pi - 0.01  (NFFT1_2D.m:11, NFFT2_2D.cu:27)
@@ -70,6 +87,7 @@ struct nfft2d_plan_s {
     double sigma = 2.0;
     nfft2d::Geom g{};
     nfft2d::WinConst w{};
+    nfft2d::WinPoly poly{};      // FP32 window polynomials
     int chunk = 256;
     int gather_variant = NFFT2D_VARIANT_TILED;
     int spread_variant = NFFT2D_VARIANT_TILED;

@@ -16,6 +16,7 @@ struct KArgs {
     int M;                   // points (direct kernels)
     int chunk;               // maximum points per work item of the chunk list
     int *status;             // [1]: latched error bits
+    WinPoly poly;            // FP32 window polynomials (kernel parameter space)
 };
 
 inline KArgs make_kargs(const nfft2d_plan_s *p) {
@@ -34,6 +35,7 @@ inline KArgs make_kargs(const nfft2d_plan_s *p) {
     a.M = static_cast<int>(p->M);
     a.chunk = p->chunk;
     a.status = p->d_status;
+    a.poly = p->poly;
     return a;
 }
 

@@ -46,6 +46,63 @@ void nfft2d::deapod_table_host(int N, int n, int K, double alpha, double *out) {
     }
 }
 
+double nfft2d::fit_window_poly(double sigma, int K, WinPoly *out) {
+    if (!out || K < kMinK || K > kMaxK || !(sigma >= 1.0) || !std::isfinite(sigma)) return -1.0;
+    const double pi = 3.141592653589793238462643383279502884;
+    const double alpha = (2.0 - 1.0 / sigma) * pi - 0.01;
+    const double cn = K / std::sinh(alpha * K);
+    // the normalised window, closed form with both branches
+    auto win = [&](double u) {
+        const double P = (K - u) * (K + u);
+        const double s = std::sqrt(std::fabs(P));
+        if (s == 0.0) return cn * alpha;
+        return cn * (P > 0 ? std::sinh(alpha * s) : std::sin(alpha * s)) / s;
+    };
+    const int D = poly_degree(K), n = D + 1;
+    std::memset(out, 0, sizeof(*out));
+    double maxerr = 0.0;
+    for (int a = 0; a <= 2 * K; ++a) {
+        const int m = a - K;
+        // interpolate at the Chebyshev nodes of [-1/2, 1/2]: Vandermonde
+        // system, Gaussian elimination with partial pivoting
+        double A[kPolyCoef][kPolyCoef + 1];
+        for (int i = 0; i < n; ++i) {
+            const double t = 0.5 * std::cos(pi * (i + 0.5) / n);
+            double pw = 1.0;
+            for (int j = 0; j < n; ++j) {
+                A[i][j] = pw;
+                pw *= t;
+            }
+            A[i][n] = win(t - m);
+        }
+        for (int col = 0; col < n; ++col) {
+            int piv = col;
+            for (int r = col + 1; r < n; ++r)
+                if (std::fabs(A[r][col]) > std::fabs(A[piv][col])) piv = r;
+            if (piv != col)
+                for (int j = 0; j <= n; ++j) std::swap(A[col][j], A[piv][j]);
+            for (int r = col + 1; r < n; ++r) {
+                const double f = A[r][col] / A[col][col];
+                for (int j = col; j <= n; ++j) A[r][j] -= f * A[col][j];
+            }
+        }
+        double c[kPolyCoef];
+        for (int i = n - 1; i >= 0; --i) {
+            double v = A[i][n];
+            for (int j = i + 1; j < n; ++j) v -= A[i][j] * c[j];
+            c[i] = v / A[i][i];
+        }
+        for (int q = 0; q <= 1000; ++q) {
+            const double t = -0.5 + q / 1000.0;
+            double v = c[D];
+            for (int d = D - 1; d >= 0; --d) v = v * t + c[d];
+            maxerr = std::max(maxerr, std::fabs(v - win(t - m)));
+        }
+        for (int d = 0; d < n; ++d) out->c[d][a] = static_cast<float>(c[d]);
+    }
+    return maxerr;
+}
+
 namespace {
 
 constexpr double kPi = 3.141592653589793238462643383279502884;
@@ -809,6 +866,8 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     p->w.alpha = alpha;
     p->w.cn = K / std::sinh(alpha * K);
     p->w.kp = K / (1.0 - std::exp(-2.0 * alpha * K));
+    const double poly_err = fit_window_poly(sigma, K, &p->poly);
+    if (!(poly_err >= 0.0 && poly_err < 1e-8)) return fail(NFFT2D_ERR_INTERNAL);
 
     const size_t rs = real_size(precision);
     cudaError_t e;

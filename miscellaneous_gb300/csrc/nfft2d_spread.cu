@@ -45,7 +45,8 @@ template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid_constant__ CUtensorMap tmap,
                                                                     const Rec32 *__restrict__ recs,
                                                                     const int4 *__restrict__ chunks,
-                                                                    const float2 *__restrict__ f, const KArgs a) {
+                                                                    const float2 *__restrict__ f,
+                                                                    const __grid_constant__ KArgs a) {
     extern __shared__ unsigned char smem_raw[];
     constexpr int PR = kRegTile + 2 * K;  // patch rows
     const Geom g = a.g;                   // g.T == kRegTile, g.PC == 32
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
         float2 acc[PR];
 #pragma unroll
         for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
-        spread_points<K>(recs, ch.y, ch.z, r0, c0, f, scr, acc, a.alpha, a.cn, a.kp, a.status);
+        spread_points<K>(recs, ch.y, ch.z, r0, c0, f, scr, acc, a.poly, a.status);
         flush_patch<K>(&tmap, patch, acc, g.H, r0, c0, pending);
         pending = true;
     }
@@ -87,7 +88,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
 
 template <int K, typename Real, typename RecT>
 __global__ void __launch_bounds__(kThreads) k_spread_direct(Real *__restrict__ grid, const RecT *__restrict__ recs,
-                                                            const Real *__restrict__ f, const KArgs a) {
+                                                            const Real *__restrict__ f,
+                                                            const __grid_constant__ KArgs a) {
     constexpr int W = 2 * K + 1;
     const int i = blockIdx.x * kThreads + threadIdx.x;
     if (i >= a.M) return;
@@ -101,8 +103,8 @@ __global__ void __launch_bounds__(kThreads) k_spread_direct(Real *__restrict__ g
     const Real vx = f[2 * static_cast<size_t>(r.orig)], vy = f[2 * static_cast<size_t>(r.orig) + 1];
     Real w1[W], w2[W];
     if constexpr (sizeof(Real) == 4) {
-        weights_f32<K>(r.t1, w1, a.alpha, a.cn, a.kp);
-        weights_f32<K>(r.t2, w2, a.alpha, a.cn, a.kp);
+        weights_poly<K>(r.t1, w1, a.poly);
+        weights_poly<K>(r.t2, w2, a.poly);
     } else {
         weights_f64<K>(r.t1, w1, a.alpha_d, a.cn_d);
         weights_f64<K>(r.t2, w2, a.alpha_d, a.cn_d);

@@ -18,11 +18,11 @@ namespace nfft2d {
 // with FMA, the sum over rows compensated (TwoSum) when COMP.
 template <int K, bool COMP>
 __device__ __forceinline__ float2 gather_point(const float2 *__restrict__ patch, int PC, int Ke, int lr, int lc,
-                                               float t1, float t2, float alpha, float cn, float kp) {
+                                               float t1, float t2, const WinPoly &wp) {
     constexpr int W = 2 * K + 1;
     float w1[W], w2[W];
-    weights_f32<K>(t1, w1, alpha, cn, kp);
-    weights_f32<K>(t2, w2, alpha, cn, kp);
+    weights_poly<K>(t1, w1, wp);
+    weights_poly<K>(t2, w2, wp);
     const float2 *base = patch + lr * PC + lc + (Ke - K);
     float sx = 0.f, sy = 0.f, ex = 0.f, ey = 0.f;
 #pragma unroll
@@ -103,8 +103,7 @@ __device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const
 template <int K>
 __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, int first, int cnt, int r0, int c0,
                                               const float2 *__restrict__ f, float *scr,
-                                              float2 (&acc)[kRegTile + 2 * K], float alpha, float cn, float kp,
-                                              int *status) {
+                                              float2 (&acc)[kRegTile + 2 * K], const WinPoly &wp, int *status) {
     constexpr int W = 2 * K + 1;
     constexpr int PR = kRegTile + 2 * K;
     constexpr int KE = K + (K & 1);
@@ -125,8 +124,8 @@ __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, in
                 v = make_float2(0.f, 0.f);  // contributes nothing
             }
             float w1[W], w2[W];
-            weights_f32<K>(__int_as_float(raw.x), w1, alpha, cn, kp);
-            weights_f32<K>(__int_as_float(raw.y), w2, alpha, cn, kp);
+            weights_poly<K>(__int_as_float(raw.x), w1, wp);
+            weights_poly<K>(__int_as_float(raw.y), w2, wp);
             float *sp = scr + lane * SP;
             reinterpret_cast<float4 *>(sp)[0] = make_float4(__int_as_float(lr), __int_as_float(lc), v.x, v.y);
 #pragma unroll

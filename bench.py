@@ -411,6 +411,10 @@ def run_ours(args, wl):
     plan = Plan(N1, N2, sigma=wl["sigma"], K=wl["K"], precision="f32", stream=stream)
     plan.set_points(x1, x2, units="unit")
     tuned = None
+    if args.no_autotune and args.gather_variant != "auto":
+        from miscellaneous_gb300 import _lib as _l
+        plan.set_tuning(gather_variant=_l.VARIANT_TILED if args.gather_variant == "tiled" else _l.VARIANT_DIRECT)
+        plan.set_points(x1, x2, units="unit")
     if not args.no_autotune:
         from miscellaneous_gb300 import autotune
         tuned = autotune.tune(plan, x1, x2, F, f, use_cache=False)  # measured here, outside the timed region
@@ -896,6 +900,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
+                    help="with --no-autotune: the gather kernel to use (default: the plan's default)")
     ap.add_argument("--K", type=int, default=None, help="window half-width for the clustered workload (4, 6, 8)")
     args = ap.parse_args()
     if args.warmup < 3:

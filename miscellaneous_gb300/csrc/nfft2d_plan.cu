@@ -587,7 +587,9 @@ int setup_grid(nfft2d_plan_s *p) {
     if (!p->grid_external) {
         cudaFree(p->grid);
         p->grid = nullptr;
-        const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C;
+        // 256 zeroed bytes of slack after the grid: the 16-byte-load gather
+        // may read one complex past the last row's end (with weight 0)
+        const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C + 256;
         NFFT_TRY_CUDA(cudaMalloc(&p->grid, bytes));
         NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, bytes, p->stream));
         int n[2] = {g.n1, g.n2};

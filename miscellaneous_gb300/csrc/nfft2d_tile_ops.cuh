@@ -5,6 +5,9 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+#include <utility>
+
 #include "nfft2d_device.cuh"
 #include "nfft2d_internal.h"
 
@@ -96,6 +99,12 @@ __device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const
 #undef NFFT2D_ROW_CASE
 }
 
+// f(integral_constant<int, L>) for L = 0, 1, ..., in order.
+template <typename F, int... Ls>
+__device__ __forceinline__ void for_each_row(F &&f, std::integer_sequence<int, Ls...>) {
+    (f(std::integral_constant<int, Ls>{}), ...);
+}
+
 // Add the contributions of points [first, first + cnt) of one tile (origin
 // r0, c0) to the warp's register patch acc (lane = patch column).  scr is the
 // warp's scratch of 32 * point_scratch<K>() floats.  A record outside the tile
@@ -134,12 +143,13 @@ __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, in
             for (int k = 0; k < WP; ++k) sp[4 + WP + k] = k < W ? w2[k] : 0.f;
         }
         __syncwarp();
-        // 2) the warp walks the points; lane = patch column
-        for (int j = 0; j < nb; ++j) {
+        // 2) the warp walks the points; lane = patch column.  Operands of
+        //    point j: row offset, the 2K+1 row weights (broadcast) and this
+        //    lane's column weight times the value.
+        auto load = [&](int j, float (&w1)[WP], float &ax, float &ay) {
             const float *sp = scr + j * SP;
             const float4 meta = reinterpret_cast<const float4 *>(sp)[0];
-            const int lr = __float_as_int(meta.x), lc = __float_as_int(meta.y);
-            float w1[WP];
+            const int lc = __float_as_int(meta.y);
 #pragma unroll
             for (int q = 0; q < WP / 4; ++q) {
                 const float4 t = reinterpret_cast<const float4 *>(sp + 4)[q];
@@ -150,7 +160,32 @@ __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, in
             }
             const int b = lane - lc - (KE - K);  // this lane's tap column
             const float w2 = (static_cast<unsigned>(b) < static_cast<unsigned>(W)) ? sp[4 + WP + b] : 0.f;
-            add_rows_switch<K, PR>(lr, acc, w1, meta.z * w2, meta.w * w2);
+            ax = meta.z * w2;
+            ay = meta.w * w2;
+        };
+        int j = 0;
+        // The binning sorts a tile's points by row, so the walk visits the
+        // row offsets in increasing order: phase L adds its run of points to
+        // acc[L .. L+2K] with compile-time register indices and no indirect
+        // branch.  (A point out of order -- only after a latched bounds
+        // error -- is left to the dispatch loop below.)
+        int lr_j = nb > 0 ? __float_as_int(scr[0]) : kRegTile;
+        for_each_row(
+            [&](auto Lc) {
+                constexpr int L = decltype(Lc)::value;
+                while (lr_j == L) {
+                    float w1[WP], ax, ay;
+                    load(j, w1, ax, ay);
+                    ++j;
+                    lr_j = j < nb ? __float_as_int(scr[j * SP]) : kRegTile;
+                    add_rows<K, PR, L>(acc, w1, ax, ay);
+                }
+            },
+            std::make_integer_sequence<int, kRegTile>{});
+        for (; j < nb; ++j) {
+            float w1[WP], ax, ay;
+            load(j, w1, ax, ay);
+            add_rows_switch<K, PR>(__float_as_int(scr[j * SP]), acc, w1, ax, ay);
         }
         __syncwarp();  // scratch is rewritten by the next batch
     }

@@ -57,15 +57,16 @@ __device__ __forceinline__ float2 gather_point(const float2 *__restrict__ patch,
 // ---------------------------------------------------------------------------
 constexpr int kRegTile = 16;  // tile edge the register-resident spread requires
 
-// Per-point scratch (floats): lr, lc, v.x, v.y, then w1 and w2, each padded
-// to a multiple of 4 floats (2K+1 used).
+// Per-point scratch (floats): lr, lc, v.x, v.y; the row weights w1 padded to
+// a multiple of 4 floats (2K+1 used); then the column products v * w2 as
+// float2, same padding.
 template <int K>
 constexpr int wpad() {
     return ((2 * K + 1 + 3) / 4) * 4;
 }
 template <int K>
 constexpr int point_scratch() {
-    return 4 + 2 * wpad<K>();
+    return 4 + 3 * wpad<K>();
 }
 
 // acc[L + a] += (ax, ay) * w1[a] for the 2K+1 rows of a point whose first
@@ -140,16 +141,17 @@ __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, in
 #pragma unroll
             for (int k = 0; k < WP; ++k) sp[4 + k] = k < W ? w1[k] : 0.f;
 #pragma unroll
-            for (int k = 0; k < WP; ++k) sp[4 + WP + k] = k < W ? w2[k] : 0.f;
+            for (int k = 0; k < WP; ++k)
+                reinterpret_cast<float2 *>(sp + 4 + WP)[k] =
+                    k < W ? make_float2(v.x * w2[k], v.y * w2[k]) : make_float2(0.f, 0.f);
         }
         __syncwarp();
         // 2) the warp walks the points; lane = patch column.  Operands of
-        //    point j: row offset, the 2K+1 row weights (broadcast) and this
-        //    lane's column weight times the value.
+        //    point j: the 2K+1 row weights (broadcast) and this lane's column
+        //    product v * w2 (zero outside the point's columns).
         auto load = [&](int j, float (&w1)[WP], float &ax, float &ay) {
             const float *sp = scr + j * SP;
-            const float4 meta = reinterpret_cast<const float4 *>(sp)[0];
-            const int lc = __float_as_int(meta.y);
+            const int lc = __float_as_int(sp[1]);
 #pragma unroll
             for (int q = 0; q < WP / 4; ++q) {
                 const float4 t = reinterpret_cast<const float4 *>(sp + 4)[q];
@@ -159,29 +161,36 @@ __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, in
                 w1[4 * q + 3] = t.w;
             }
             const int b = lane - lc - (KE - K);  // this lane's tap column
-            const float w2 = (static_cast<unsigned>(b) < static_cast<unsigned>(W)) ? sp[4 + WP + b] : 0.f;
-            ax = meta.z * w2;
-            ay = meta.w * w2;
+            const float2 vw = (static_cast<unsigned>(b) < static_cast<unsigned>(W))
+                                  ? reinterpret_cast<const float2 *>(sp + 4 + WP)[b] : make_float2(0.f, 0.f);
+            ax = vw.x;
+            ay = vw.y;
         };
         int j = 0;
         // The binning sorts a tile's points by row, so the walk visits the
-        // row offsets in increasing order: phase L adds its run of points to
-        // acc[L .. L+2K] with compile-time register indices and no indirect
-        // branch.  (A point out of order -- only after a latched bounds
-        // error -- is left to the dispatch loop below.)
-        int lr_j = nb > 0 ? __float_as_int(scr[0]) : kRegTile;
-        for_each_row(
-            [&](auto Lc) {
-                constexpr int L = decltype(Lc)::value;
-                while (lr_j == L) {
-                    float w1[WP], ax, ay;
-                    load(j, w1, ax, ay);
-                    ++j;
-                    lr_j = j < nb ? __float_as_int(scr[j * SP]) : kRegTile;
-                    add_rows<K, PR, L>(acc, w1, ax, ay);
-                }
-            },
-            std::make_integer_sequence<int, kRegTile>{});
+        // row offsets in increasing order: phase L adds its run of points
+        // (counted by one ballot) to acc[L .. L+2K] with compile-time
+        // register indices and no indirect branch.  A batch out of order --
+        // only after a latched bounds error -- goes through the dispatch
+        // loop below instead.
+        {
+            const int my_lr = lane < nb ? __float_as_int(scr[lane * SP]) : kRegTile;
+            const int prev = __shfl_up_sync(0xffffffffu, my_lr, 1);
+            const bool sorted = __all_sync(0xffffffffu, lane == 0 || prev <= my_lr);
+            if (sorted) {
+                for_each_row(
+                    [&](auto Lc) {
+                        constexpr int L = decltype(Lc)::value;
+                        const int e = j + __popc(__ballot_sync(0xffffffffu, my_lr == L));
+                        for (; j < e; ++j) {
+                            float w1[WP], ax, ay;
+                            load(j, w1, ax, ay);
+                            add_rows<K, PR, L>(acc, w1, ax, ay);
+                        }
+                    },
+                    std::make_integer_sequence<int, kRegTile>{});
+            }
+        }
         for (; j < nb; ++j) {
             float w1[WP], ax, ay;
             load(j, w1, ax, ay);

@@ -494,17 +494,32 @@ def run_ours(args, wl):
         dx1, dx2 = torch.empty_like(x1), torch.empty_like(x2)
         dF, df = torch.empty_like(F), torch.empty_like(f)
         plan.enable_timing(False)
+        # the copies that the compute does not wait for run on a second
+        # stream: F and f go up while set_points bins the points, f_out comes
+        # down while the adjoint runs
+        cs = torch.cuda.Stream(device=dev)
+        ev_start, ev_in, ev_fwd, ev_out = (torch.cuda.Event() for _ in range(4))
 
         def e2e_step():
+            ev_start.record(stream)
             dx1.copy_(hx1, non_blocking=True)
             dx2.copy_(hx2, non_blocking=True)
-            dF.copy_(hF, non_blocking=True)
-            df.copy_(hf, non_blocking=True)
+            cs.wait_event(ev_start)
+            with torch.cuda.stream(cs):
+                dF.copy_(hF, non_blocking=True)
+                df.copy_(hf, non_blocking=True)
+                ev_in.record(cs)
             plan.set_points(dx1, dx2, units="unit")
+            stream.wait_event(ev_in)
             plan.forward(dF, out=f_out)
+            ev_fwd.record(stream)
             plan.adjoint(df, out=F_out)
-            hf_out.copy_(f_out, non_blocking=True)
+            cs.wait_event(ev_fwd)
+            with torch.cuda.stream(cs):
+                hf_out.copy_(f_out, non_blocking=True)
+                ev_out.record(cs)
             hF_out.copy_(F_out, non_blocking=True)
+            stream.wait_event(ev_out)
 
         for _ in range(args.warmup):
             e2e_step()
@@ -525,7 +540,8 @@ def run_ours(args, wl):
         d2h = hf_out.numel() * 8 + hF_out.numel() * 8
         e2e = {"value": world * M / (te * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te,
-               "includes": "H2D copies, set_points (binning sort), forward, adjoint, D2H copies"}
+               "includes": "H2D copies, set_points (binning sort), forward, adjoint, D2H copies; the F/f uploads "
+                           "overlap set_points and the f download overlaps the adjoint (second stream)"}
         # restore the resident plan state for the accuracy check
         plan.set_points(x1, x2, units="unit")
 

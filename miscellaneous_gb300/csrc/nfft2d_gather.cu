@@ -15,7 +15,8 @@
 // (TwoSum) when enabled.
 //
 // DIRECT variant (both precisions): one thread per sorted point reads its
-// taps straight from the padded grid (L1/L2), no shared memory.
+// taps straight from the padded grid (L1/L2), no shared memory; FP32 reads
+// two taps per 16-byte load.
 #include <cuda.h>
 #include <cuda_runtime.h>
 

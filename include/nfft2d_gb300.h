@@ -99,6 +99,11 @@ typedef struct {
     int gather_variant;    /* NFFT2D_VARIANT_*                                  */
     int spread_variant;    /* NFFT2D_VARIANT_*                                  */
     int compensated;       /* -1 = default (on); 0 off; 1 on (FP32 gather)      */
+    int fft_pruned;        /* -1 = keep (initially: by grid size, two passes from
+                              2048 x 2048 oversampled cells up); 0: one 2D cuFFT
+                              plan; 1: two 1D passes, the column pass only over
+                              the columns the band needs (1.5 instead of 2
+                              passes at sigma = 2)                              */
 } nfft2d_tuning;
 
 /* Stage times in milliseconds, from CUDA events recorded on the plan's

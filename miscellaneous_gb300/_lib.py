@@ -53,7 +53,7 @@ class Info(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int), ("chunk", ctypes.c_int), ("gather_variant", ctypes.c_int),
-                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int)]
+                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int), ("fft_pruned", ctypes.c_int)]
 
 
 class Timings(ctypes.Structure):

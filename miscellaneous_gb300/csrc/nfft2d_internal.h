@@ -122,6 +122,9 @@ struct nfft2d_plan_s {
 
     cufftHandle fft = 0;
     bool fft_ok = false;
+    cufftHandle fft_rows = 0, fft_cols = 0;  // pruned 1D passes (see run_fft)
+    bool pruned_ok = false;
+    int fft_pruned = -1;                     // 1 use them, 0 don't, -1 by grid size
     CUtensorMap tmap;  // 64-byte aligned by its own declaration
     bool tmap_ok = false;
 

@@ -532,6 +532,10 @@ void free_points(nfft2d_plan_s *p) {
 void destroy_plan(nfft2d_plan_s *p) {
     if (!p) return;
     if (p->fft_ok) cufftDestroy(p->fft);
+    if (p->pruned_ok) {
+        cufftDestroy(p->fft_rows);
+        cufftDestroy(p->fft_cols);
+    }
     free_points(p);
     if (!p->grid_external) cudaFree(p->grid);
     cudaFree(p->deap1);
@@ -583,6 +587,11 @@ int setup_grid(nfft2d_plan_s *p) {
         cufftDestroy(p->fft);
         p->fft_ok = false;
     }
+    if (p->pruned_ok) {
+        cufftDestroy(p->fft_rows);
+        cufftDestroy(p->fft_cols);
+        p->pruned_ok = false;
+    }
     p->tmap_ok = false;
     if (!p->grid_external) {
         cudaFree(p->grid);
@@ -600,6 +609,23 @@ int setup_grid(nfft2d_plan_s *p) {
         if (fr != CUFFT_SUCCESS) return status_from_cufft(fr);
         p->fft_ok = true;
         if ((fr = cufftSetStream(p->fft, p->stream)) != CUFFT_SUCCESS) return status_from_cufft(fr);
+        // the pruned pair: n1 rows of n2 points (contiguous, pitch C), and
+        // N2/2 columns of n1 points (stride C) run once per half of the band
+        const cufftType t = p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C;
+        int nr[1] = {g.n2}, er[1] = {g.C};
+        int nc[1] = {g.n1}, ec[1] = {g.Ra};
+        if (cufftPlanMany(&p->fft_rows, 1, nr, er, 1, g.C, er, 1, g.C, t, g.n1) == CUFFT_SUCCESS) {
+            if (cufftPlanMany(&p->fft_cols, 1, nc, ec, g.C, 1, ec, g.C, 1, t, p->N2 / 2) == CUFFT_SUCCESS) {
+                p->pruned_ok = cufftSetStream(p->fft_rows, p->stream) == CUFFT_SUCCESS &&
+                               cufftSetStream(p->fft_cols, p->stream) == CUFFT_SUCCESS;
+                if (!p->pruned_ok) {
+                    cufftDestroy(p->fft_rows);
+                    cufftDestroy(p->fft_cols);
+                }
+            } else {
+                cufftDestroy(p->fft_rows);
+            }
+        }
     }
     if (p->precision == NFFT2D_F32) return make_tensor_map(p);
     return NFFT2D_OK;
@@ -745,19 +771,43 @@ cudaError_t launch_halo_fold(const nfft2d_plan_s *p) {
 // ===========================================================================
 namespace {
 
-int run_fft(nfft2d_plan_s *p, int sign) {
+// One in-place C2C / Z2Z transform (a 1D batch or the full 2D plan) at
+// element offset off of the grid.
+cufftResult exec_at(const nfft2d_plan_s *p, cufftHandle h, size_t off, int dir) {
+    if (p->precision == NFFT2D_F64) {
+        cufftDoubleComplex *d = static_cast<cufftDoubleComplex *>(p->grid) + off;
+        return cufftExecZ2Z(h, d, d, dir);
+    }
+    cufftComplex *d = static_cast<cufftComplex *>(p->grid) + off;
+    return cufftExecC2C(h, d, d, dir);
+}
+
+// The oversampled FFT.  With the pruned plans the 2D transform runs as two
+// 1D passes and the column pass covers only the columns that matter: for a
+// type-2 transform (type2 = true) the padded coefficients are zero outside
+// the band |k2| < N2/2, so only those columns are transformed (first), then
+// every row; for a type-1 transform every row is transformed first and only
+// the columns the crop keeps afterwards.  With sigma = 2 that is 1.5 passes
+// over the grid instead of 2.
+int run_fft(nfft2d_plan_s *p, int sign, bool type2) {
     const Geom &g = p->g;
     const int dir = sign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
     const size_t off = static_cast<size_t>(g.H) * g.C + g.H;
+    // by default the two passes run from 2048 x 2048 oversampled cells up:
+    // below that cuFFT's single 2D plan is faster on GB300 (1024^2: 20 us
+    // vs 30 us; 2048^2: 40 vs 35 us; 4096^2: 153 vs 112 us)
+    const bool pruned = p->fft_pruned > 0 || (p->fft_pruned < 0 && 1LL * g.n1 * g.n2 >= 2048LL * 2048LL);
+    if (!(pruned && p->pruned_ok)) return status_from_cufft(exec_at(p, p->fft, off, dir));
+    const size_t right = off + static_cast<size_t>(g.n2 - p->N2 / 2);  // first column of the negative band
     cufftResult r;
-    if (p->precision == NFFT2D_F64) {
-        cufftDoubleComplex *d = static_cast<cufftDoubleComplex *>(p->grid) + off;
-        r = cufftExecZ2Z(p->fft, d, d, dir);
-    } else {
-        cufftComplex *d = static_cast<cufftComplex *>(p->grid) + off;
-        r = cufftExecC2C(p->fft, d, d, dir);
+    if (type2) {
+        if ((r = exec_at(p, p->fft_cols, off, dir)) != CUFFT_SUCCESS) return status_from_cufft(r);
+        if ((r = exec_at(p, p->fft_cols, right, dir)) != CUFFT_SUCCESS) return status_from_cufft(r);
+        return status_from_cufft(exec_at(p, p->fft_rows, off, dir));
     }
-    return status_from_cufft(r);
+    if ((r = exec_at(p, p->fft_rows, off, dir)) != CUFFT_SUCCESS) return status_from_cufft(r);
+    if ((r = exec_at(p, p->fft_cols, off, dir)) != CUFFT_SUCCESS) return status_from_cufft(r);
+    return status_from_cufft(exec_at(p, p->fft_cols, right, dir));
 }
 
 int type2_prepare(nfft2d_plan_s *p, int sign, const void *F) {
@@ -765,7 +815,7 @@ int type2_prepare(nfft2d_plan_s *p, int sign, const void *F) {
     NFFT_TRY_CUDA(launch_pad(p, F));
     stage_end(p, ST_PAD);
     stage_begin(p, ST_FFT2);
-    int st = run_fft(p, sign);
+    int st = run_fft(p, sign, true);
     if (st != NFFT2D_OK) return st;
     stage_end(p, ST_FFT2);
     stage_begin(p, ST_FILL);
@@ -928,6 +978,11 @@ int nfft2d_plan_destroy(nfft2d_plan p) {
 int nfft2d_set_stream(nfft2d_plan p, void *stream) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
     p->stream = static_cast<cudaStream_t>(stream);
+    if (p->pruned_ok) {
+        cufftResult r = cufftSetStream(p->fft_rows, p->stream);
+        if (r == CUFFT_SUCCESS) r = cufftSetStream(p->fft_cols, p->stream);
+        if (r != CUFFT_SUCCESS) return status_from_cufft(r);
+    }
     return status_from_cufft(cufftSetStream(p->fft, p->stream));
 }
 
@@ -963,6 +1018,7 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     p->gather_variant = gv;
     p->spread_variant = sv;
     if (t->compensated >= 0) p->compensated = t->compensated ? 1 : 0;
+    if (t->fft_pruned >= 0) p->fft_pruned = t->fft_pruned ? 1 : 0;
     p->workspace_bytes = plan_workspace_bytes(p);
     return NFFT2D_OK;
 }
@@ -1105,7 +1161,7 @@ int nfft2d::type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const
     NFFT_TRY_CUDA(pad(p, ctx));
     stage_end(p, ST_PAD);
     stage_begin(p, ST_FFT2);
-    int st = run_fft(p, sign);
+    int st = run_fft(p, sign, true);
     if (st != NFFT2D_OK) return st;
     stage_end(p, ST_FFT2);
     stage_begin(p, ST_FILL);
@@ -1152,7 +1208,7 @@ static int nfft2d_type1_impl(nfft2d_plan p, int sign, const void *f, void *F) {
     NFFT_TRY_CUDA(launch_halo_fold(p));
     stage_end(p, ST_FOLD);
     stage_begin(p, ST_FFT1);
-    int st = run_fft(p, sign);
+    int st = run_fft(p, sign, false);
     if (st != NFFT2D_OK) return st;
     stage_end(p, ST_FFT1);
     stage_begin(p, ST_CROP);

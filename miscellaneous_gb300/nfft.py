@@ -102,8 +102,8 @@ class Plan:
         check(self._lib.nfft2d_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "nfft2d_set_stream")
 
     def set_tuning(self, tile: int = 0, chunk: int = 0, gather_variant: int = 0, spread_variant: int = 0,
-                   compensated: int = -1) -> None:
-        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated)
+                   compensated: int = -1, fft_pruned: int = -1) -> None:
+        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated, fft_pruned)
         check(self._lib.nfft2d_set_tuning(self._h, ctypes.byref(t)), "nfft2d_set_tuning")
 
     def info(self) -> dict:

@@ -141,16 +141,28 @@ __device__ __forceinline__ void weights_f32(float t, float (&w)[2 * K + 1], floa
 
 // All 2K+1 taps from the plan's polynomials: Horner steps on FP32 FMAs whose
 // coefficients are read from kernel parameter space (uniform across the warp).
+// Taps (2j, 2j+1) share one packed FP32x2 FMA (__ffma2_rn) per Horner step;
+// the odd last tap runs alone.
 template <int K>
 __device__ __forceinline__ void weights_poly(float t, float (&w)[2 * K + 1], const WinPoly &P) {
     constexpr int D = poly_degree(K);
+    const float2 tt = make_float2(t, t);
+    float2 acc[K];
+    float last = P.c[D][2 * K];
 #pragma unroll
-    for (int a = 0; a <= 2 * K; ++a) w[a] = P.c[D][a];
+    for (int j = 0; j < K; ++j) acc[j] = *reinterpret_cast<const float2 *>(&P.c[D][2 * j]);
 #pragma unroll
     for (int d = D - 1; d >= 0; --d) {
 #pragma unroll
-        for (int a = 0; a <= 2 * K; ++a) w[a] = fmaf(w[a], t, P.c[d][a]);
+        for (int j = 0; j < K; ++j) acc[j] = __ffma2_rn(acc[j], tt, *reinterpret_cast<const float2 *>(&P.c[d][2 * j]));
+        last = fmaf(last, t, P.c[d][2 * K]);
     }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        w[2 * j] = acc[j].x;
+        w[2 * j + 1] = acc[j].y;
+    }
+    w[2 * K] = last;
 }
 
 // Derivative dw/dt of the same taps (d/dt of w(t - m)).

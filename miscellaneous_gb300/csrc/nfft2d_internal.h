@@ -44,8 +44,8 @@ struct __align__(8) Rec64 {
 // FINUFFT by Barnett, Magland and af Klinteberg, SIAM J. Sci. Comput. 2019).
 constexpr int kPolyCoef = 11;
 __host__ __device__ constexpr int poly_degree(int K) { return K <= 3 ? 10 : 9; }
-struct WinPoly {
-    float c[kPolyCoef][2 * kMaxK + 1];
+struct __align__(8) WinPoly {
+    float c[kPolyCoef][2 * kMaxK + 2];  // rows padded to an even length: tap pairs are 8-byte aligned
 };
 
 // Fit the polynomials of the window for (sigma, K); returns the max abs

@@ -146,8 +146,22 @@ def uneven_batch(seed: int = 3, count: int = 64):
                         "w": 6, "seed": seed})
 
 
+def pso_batch(seed: int = 6, count: int = 250, N: int = 44, M: int = 44 * 44):
+    """The PSO reflectarray synthesis shape: one transform per particle per
+    generation -- 250 particles (Synthesis/PSO/PSO.cu:27), a 44 x 44 element
+    array (kernel_single_v2.cu:30-31, M = 1936 points) onto the 2Nu x 2Nv =
+    44 x 44 spectral grid -- which the reference runs as one NFFT2_2D_GPU call
+    per particle (Synthesis.cu:395).  Points uniform, coefficients N(0,1)
+    complex; sigma 2, w 6."""
+    items = [dict(N=N, M=M) for _ in range(count)]
+    return dict(name=f"pso_batch_{count}x{N}x{N}_{M}", items=items, seed=seed, sigma=2.0, K=6,
+                config={"workload": "PSO far-field batch: one small transform per particle", "count": count,
+                        "N": [N, N], "points_per_transform": M, "points": count * M, "sigma": 2.0, "w": 6,
+                        "seed": seed})
+
+
 WORKLOADS = {"polar": polar_raster, "config1": uniform_config1, "clustered": clustered_config3, "batch": uneven_batch,
-             "lsq": least_squares_config5, "knab": knab_regrid}
+             "lsq": least_squares_config5, "knab": knab_regrid, "pso": pso_batch}
 
 
 # ---------------------------------------------------------------------------
@@ -933,9 +947,9 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the least-squares workload has no reference counterpart"}))
             return
         run_lsq(args, wl)
-    elif args.workload == "batch":
+    elif args.workload in ("batch", "pso"):
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no reference counterpart"}))
+            print(json.dumps({"impl": "reference", "unavailable": "the batch workloads have no reference counterpart"}))
             return
         run_batch(args, wl)
     elif args.impl == "reference":

@@ -68,3 +68,27 @@ def test_batch_rebinning_recaptures_the_graph(orc):
             for t, ((n1, n2), x, F) in enumerate(zip(sizes, xs, Fs)):
                 g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
                 assert orc.rel_l2(outs[t].cpu().numpy(), orc.ndft_type2(F, g1, g2, sign=-1)) < 1e-5
+
+
+def test_pso_shaped_batch_matches_single_plans():
+    """The PSO synthesis shape: 250 transforms of 1936 points on a 44 x 44
+    grid (a grid that is not a whole number of 16 x 16 tiles), replayed twice
+    from the captured graph."""
+    from miscellaneous_gb300.nfft import Batch
+    sizes = [(44, 44)] * 250
+    Ms = [44 * 44] * 250
+    xs, Fs, fs = _problem(sizes, Ms, seed=250)
+    b = Batch(sizes)
+    b.set_points([torch.from_numpy(x[0]).cuda() for x in xs], [torch.from_numpy(x[1]).cuda() for x in xs])
+    Ft = [torch.from_numpy(F).cuda().reshape(-1) for F in Fs]
+    ft = [torch.from_numpy(f).cuda() for f in fs]
+    for _ in range(2):
+        outs_f = b.forward(Ft)
+        outs_F = b.adjoint(ft)
+        b.synchronize()
+    for t in (0, 1, 77, 249):
+        a, c = _single(44, 44, xs[t], Fs[t], fs[t])
+        of, oF = outs_f[t].cpu().numpy(), outs_F[t].cpu().numpy().reshape(-1)
+        assert np.linalg.norm(of - a) / np.linalg.norm(a) < 1e-6
+        assert np.linalg.norm(oF - c) / np.linalg.norm(c) < 1e-6
+    b.close()

@@ -205,6 +205,11 @@ int nfft2d_batch_set_points(nfft2d_batch batch, const long long *M, const void *
                             int coord_dtype, int units);
 int nfft2d_batch_forward(nfft2d_batch batch, const void *const *F, void *const *f);
 int nfft2d_batch_adjoint(nfft2d_batch batch, const void *const *f, void *const *F);
+/* Type 1 with the reference's sign (NFFT2_2D_GPU, NFFT/NFFT2_2D.cu:329-495)
+ * for every transform of the batch: the per-particle far-field call of the
+ * PSO synthesis (Synthesis/PSO/Synthesis.cu:395) done for all particles at
+ * once. */
+int nfft2d_batch_spread_ref(nfft2d_batch batch, const void *const *f, void *const *F);
 int nfft2d_batch_set_graph(nfft2d_batch batch, int on);
 int nfft2d_batch_synchronize(nfft2d_batch batch);
 

@@ -115,6 +115,7 @@ _SIGNATURES = {
     "nfft2d_batch_set_points": (_I, [_P, _P, _P, _P, _I, _I]),
     "nfft2d_batch_forward": (_I, [_P, _P, _P]),
     "nfft2d_batch_adjoint": (_I, [_P, _P, _P]),
+    "nfft2d_batch_spread_ref": (_I, [_P, _P, _P]),
     "nfft2d_batch_set_graph": (_I, [_P, _I]),
     "nfft2d_batch_synchronize": (_I, [_P]),
     "nfft2d_knab_window": (_I, [_D, _D, _I, _I, _P, _I, ctypes.POINTER(_I)]),

@@ -333,7 +333,7 @@ struct nfft2d_batch_s {
     int total_chunks = 0, total_rows = 0, total_crop = 0;
     bool points_valid = false;
     bool use_graph = true;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0] type-2 forward, [1] type-1 adjoint
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // type-2 forward, type-1 adjoint, type-1 sign -1
     cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_io = nullptr;
     bool io_pending = false;
     Geom g0{};
@@ -390,6 +390,8 @@ int run_ffts(nfft2d_batch_s *b, int dir) {
     return NFFT2D_OK;
 }
 
+// type 2: forward (type 2, sign -1); type 1: adjoint (type 1, sign +1);
+// type -1: the reference's spreading NFFT2_2D (type 1, sign -1).
 template <int K>
 int enqueue_stages(nfft2d_batch_s *b, int type) {
     const int n = b->count;
@@ -434,7 +436,7 @@ int enqueue_stages(nfft2d_batch_s *b, int type) {
         }
         k_batch_fold<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
         B_TRY(cudaGetLastError());
-        int st = run_ffts(b, CUFFT_INVERSE);
+        int st = run_ffts(b, type == 1 ? CUFFT_INVERSE : CUFFT_FORWARD);
         if (st != NFFT2D_OK) return st;
         k_batch_crop<<<b->total_crop, kThreads, 0, b->stream>>>(b->d_desc, n, b->d_io);
         B_TRY(cudaGetLastError());
@@ -476,7 +478,7 @@ int run(nfft2d_batch_s *b, int type, const void *const *in, void *const *out) {
     B_TRY(cudaMemcpyAsync(b->d_io, b->h_io, sizeof(BatchIO) * b->count, cudaMemcpyHostToDevice, b->stream));
     B_TRY(cudaEventRecord(b->ev_io, b->stream));
     b->io_pending = true;
-    const int gi = type == 2 ? 0 : 1;
+    const int gi = type == 2 ? 0 : (type == 1 ? 1 : 2);
     if (b->use_graph) {
         if (!b->graph[gi]) {
             cudaGraph_t graph = nullptr;
@@ -629,6 +631,8 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
 int nfft2d_batch_forward(nfft2d_batch b, const void *const *F, void *const *f) { return run(b, 2, F, f); }
 
 int nfft2d_batch_adjoint(nfft2d_batch b, const void *const *f, void *const *F) { return run(b, 1, f, F); }
+
+int nfft2d_batch_spread_ref(nfft2d_batch b, const void *const *f, void *const *F) { return run(b, -1, f, F); }
 
 int nfft2d_batch_set_graph(nfft2d_batch b, int on) {
     if (!b) return NFFT2D_ERR_INVALID_ARG;

@@ -261,6 +261,15 @@ class Batch:
         check(self._lib.nfft2d_batch_adjoint(self._h, self._ptrs(fs), self._ptrs(outs)), "nfft2d_batch_adjoint")
         return outs
 
+    def spread_ref(self, fs, outs=None):
+        """Type 1 with the reference's sign (NFFT2_2D_GPU) for every transform."""
+        for m, f in zip(self.M, fs):
+            _require_cuda(f, "f", torch.complex64, m)
+        if outs is None:
+            outs = [torch.empty(n1 * n2, dtype=torch.complex64, device=fs[0].device) for n1, n2 in self.sizes]
+        check(self._lib.nfft2d_batch_spread_ref(self._h, self._ptrs(fs), self._ptrs(outs)), "nfft2d_batch_spread_ref")
+        return outs
+
     def synchronize(self) -> None:
         check(self._lib.nfft2d_batch_synchronize(self._h), "nfft2d_batch_synchronize")
 

@@ -85,10 +85,17 @@ def test_pso_shaped_batch_matches_single_plans():
     for _ in range(2):
         outs_f = b.forward(Ft)
         outs_F = b.adjoint(ft)
+        outs_R = b.spread_ref(ft)   # the reference's own sign, as its PSO code calls it
         b.synchronize()
+    from miscellaneous_gb300.nfft import Plan
     for t in (0, 1, 77, 249):
         a, c = _single(44, 44, xs[t], Fs[t], fs[t])
         of, oF = outs_f[t].cpu().numpy(), outs_F[t].cpu().numpy().reshape(-1)
         assert np.linalg.norm(of - a) / np.linalg.norm(a) < 1e-6
         assert np.linalg.norm(oF - c) / np.linalg.norm(c) < 1e-6
+        with Plan(44, 44) as p:
+            p.set_points(torch.from_numpy(xs[t][0]).cuda(), torch.from_numpy(xs[t][1]).cuda())
+            r = p.spread_ref(torch.from_numpy(fs[t]).cuda()).reshape(-1).cpu().numpy()
+        oR = outs_R[t].cpu().numpy().reshape(-1)
+        assert np.linalg.norm(oR - r) / np.linalg.norm(r) < 1e-6
     b.close()

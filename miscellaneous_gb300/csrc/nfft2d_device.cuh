@@ -165,7 +165,44 @@ __device__ __forceinline__ void weights_poly(float t, float (&w)[2 * K + 1], con
     w[2 * K] = last;
 }
 
-// Derivative dw/dt of the same taps (d/dt of w(t - m)).
+// The taps and their derivatives d/dt from the same polynomials: Horner for
+// value and slope together (slope = slope * t + value before each value
+// step), two taps per packed FMA.  The slope of the fit differs from the
+// closed form by less than 1e-7 of the window's peak slope.
+template <int K>
+__device__ __forceinline__ void weights_poly_d(float t, float (&w)[2 * K + 1], float (&dw)[2 * K + 1],
+                                               const WinPoly &P) {
+    constexpr int D = poly_degree(K);
+    const float2 tt = make_float2(t, t);
+    float2 acc[K], dacc[K];
+    float last = P.c[D][2 * K], dlast = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        acc[j] = *reinterpret_cast<const float2 *>(&P.c[D][2 * j]);
+        dacc[j] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int d = D - 1; d >= 0; --d) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            dacc[j] = __ffma2_rn(dacc[j], tt, acc[j]);
+            acc[j] = __ffma2_rn(acc[j], tt, *reinterpret_cast<const float2 *>(&P.c[d][2 * j]));
+        }
+        dlast = fmaf(dlast, t, last);
+        last = fmaf(last, t, P.c[d][2 * K]);
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        w[2 * j] = acc[j].x;
+        w[2 * j + 1] = acc[j].y;
+        dw[2 * j] = dacc[j].x;
+        dw[2 * j + 1] = dacc[j].y;
+    }
+    w[2 * K] = last;
+    dw[2 * K] = dlast;
+}
+
+// Derivative dw/dt of the same taps (d/dt of w(t - m)), closed form.
 //   interior: dw/du = w * (alpha s coth(alpha s) - 1) * (-u) / s^2
 //   edge:     dw/du = cn * g'(P) * (-2u),  g(P) = sinh(alpha sqrt(P))/sqrt(P),
 //             g' by its series near P = 0, closed forms elsewhere.

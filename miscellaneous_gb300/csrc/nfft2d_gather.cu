@@ -112,11 +112,9 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                 out[raw.w] = gather_point<K, COMP>(patch, PC, g.Ke, lr, lc, t1, t2, a.poly);
             } else {
                 float w1[W], w2[W], d1[W], d2[W];
-                weights_poly<K>(t1, w1, a.poly);
-                weights_poly<K>(t2, w2, a.poly);
+                weights_poly_d<K>(t1, w1, d1, a.poly);
+                weights_poly_d<K>(t2, w2, d2, a.poly);
                 const float2 *base = patch + lr * PC + lc + (g.Ke - K);
-                dweights_f32<K>(t1, w1, d1, a.alpha, a.cn);
-                dweights_f32<K>(t2, w2, d2, a.alpha, a.cn);
                 float ax = 0.f, ay = 0.f, bx = 0.f, by = 0.f;
 #pragma unroll
                 for (int r = 0; r < W; ++r) {
@@ -163,11 +161,12 @@ __device__ __forceinline__ void weights_any(Real t, Real (&w)[2 * K + 1], const 
         weights_f64<K>(t, w, a.alpha_d, a.cn_d);
 }
 
+// Slopes dw/dt of the taps; the FP32 path re-evaluates w with them (the
+// same Horner steps, so w is unchanged).
 template <int K, typename Real>
-__device__ __forceinline__ void dweights_any(Real t, const Real (&w)[2 * K + 1], Real (&dw)[2 * K + 1],
-                                             const KArgs &a) {
+__device__ __forceinline__ void dweights_any(Real t, Real (&w)[2 * K + 1], Real (&dw)[2 * K + 1], const KArgs &a) {
     if constexpr (sizeof(Real) == 4)
-        dweights_f32<K>(t, w, dw, a.alpha, a.cn);
+        weights_poly_d<K>(t, w, dw, a.poly);
     else
         dweights_f64<K>(t, dw, a.alpha_d, a.cn_d);
 }

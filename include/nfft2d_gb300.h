@@ -174,6 +174,12 @@ int nfft2d_enable_timing(nfft2d_plan plan, int on);
 int nfft2d_get_timings(nfft2d_plan plan, nfft2d_timings *t);
 const char *nfft2d_status_string(int status);
 int nfft2d_device_count(void);
+/* Self-test of the bounded device-side waits (no reference counterpart): one
+ * thread polls an mbarrier phase that nothing completes, gives up after
+ * spin_limit polls -- as the tiled kernels do after their own limit -- and
+ * the call returns NFFT2D_ERR_DEVICE_TIMEOUT with the context intact.
+ * Synchronizes `stream`. */
+int nfft2d_selftest_wait_timeout(int spin_limit, void *stream);
 
 /* ---- exact direct sum ----------------------------------------------------
  * Matrix-free FP64 replacement of NDFT2_2D_GPU (NFFT/NDFT2_2D.cu:37-72):

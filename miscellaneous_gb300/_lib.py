@@ -108,6 +108,7 @@ _SIGNATURES = {
     "nfft2d_get_timings": (_I, [_P, ctypes.POINTER(Timings)]),
     "nfft2d_status_string": (ctypes.c_char_p, [_I]),
     "nfft2d_device_count": (_I, []),
+    "nfft2d_selftest_wait_timeout": (_I, [_I, _P]),
     "nfft2d_ndft2d_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _LL, _LL, _I, _P]),
     "nfft2d_forward_small_noalloc": (_I, [_I, _I, _I, _LL, _P, _P, _I, _P, _P, _P]),
     "nfft2d_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _P, _D, _I, _P]),

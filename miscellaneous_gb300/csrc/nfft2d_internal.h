@@ -176,6 +176,10 @@ int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void 
 typedef cudaError_t (*PadFn)(const nfft2d_plan_s *p, const void *ctx);
 int type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const void *ctx);
 
+// cudaMalloc for plan buffers, with the host-side allocation-failure hook
+// used by the tests (see nfft2d_plan.cu).
+cudaError_t plan_malloc(void **ptr, size_t bytes);
+
 // Host FP64 helpers shared by the plan and the Knab regridder.
 double bessel_i0_host(double x);
 void deapod_table_host(int N, int n, int K, double alpha, double *out);

@@ -14,7 +14,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
+#include <mutex>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "nfft2d_device.cuh"
@@ -101,6 +104,30 @@ double nfft2d::fit_window_poly(double sigma, int K, WinPoly *out) {
         for (int d = 0; d < n; ++d) out->c[d][a] = static_cast<float>(c[d]);
     }
     return maxerr;
+}
+
+// Device allocations of a plan.  For tests of the host-side failure paths,
+// NFFT2D_FAIL_ALLOC_AT=k makes the k-th allocation (counted from the moment
+// the variable takes that value) report cudaErrorMemoryAllocation without
+// allocating; unset, it is one getenv per allocation (plan creation and
+// set_points only, never per transform).
+cudaError_t nfft2d::plan_malloc(void **ptr, size_t bytes) {
+    static std::mutex mu;
+    static std::string seen;
+    static long long count = 0;
+    const char *v = std::getenv("NFFT2D_FAIL_ALLOC_AT");
+    if (v && *v) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (seen != v) {
+            seen = v;
+            count = 0;
+        }
+        if (++count == std::atoll(v)) {
+            *ptr = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+    }
+    return cudaMalloc(ptr, bytes);
 }
 
 namespace {
@@ -590,11 +617,11 @@ int ensure_points_capacity(nfft2d_plan_s *p, long long M) {
     free_points(p);
     const long long cap = std::max<long long>(M, 1);
     const size_t rs = rec_size(p->precision);
-    NFFT_TRY_CUDA(cudaMalloc(&p->recs, rs * cap));
-    NFFT_TRY_CUDA(cudaMalloc(&p->tmp_recs, rs * cap));
-    NFFT_TRY_CUDA(cudaMalloc(&p->ranks, sizeof(unsigned) * cap));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->recs), rs * cap));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->tmp_recs), rs * cap));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->ranks), sizeof(unsigned) * cap));
     const long long cc = chunks_capacity(p, cap);
-    NFFT_TRY_CUDA(cudaMalloc(&p->chunks, sizeof(int4) * cc));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->chunks), sizeof(int4) * cc));
     p->capM = cap;
     p->chunks_cap = cc;
     return NFFT2D_OK;
@@ -630,7 +657,7 @@ int setup_grid(nfft2d_plan_s *p) {
         // 256 zeroed bytes of slack after the grid: the 16-byte-load gather
         // may read one complex past the last row's end (with weight 0)
         const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C + 256;
-        NFFT_TRY_CUDA(cudaMalloc(&p->grid, bytes));
+        NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->grid), bytes));
         NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, bytes, p->stream));
         int n[2] = {g.n1, g.n2};
         int emb[2] = {g.Ra, g.C};
@@ -672,12 +699,25 @@ int setup_bins(nfft2d_plan_s *p) {
     p->ncells = static_cast<size_t>(g.tiles1) * g.tiles2 * g.T * g.T;
     const int ntiles = g.tiles1 * g.tiles2;
     p->scan_tmp_elems = std::max(scan_tmp_needed(p->ncells + 1), scan_tmp_needed(ntiles + 1));
-    NFFT_TRY_CUDA(cudaMalloc(&p->cell_count, sizeof(unsigned) * (p->ncells + 1)));
-    NFFT_TRY_CUDA(cudaMalloc(&p->tile_chunks, sizeof(unsigned) * (ntiles + 1)));
-    NFFT_TRY_CUDA(cudaMalloc(&p->scan_tmp, sizeof(unsigned) * p->scan_tmp_elems));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->cell_count), sizeof(unsigned) * (p->ncells + 1)));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->tile_chunks), sizeof(unsigned) * (ntiles + 1)));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->scan_tmp), sizeof(unsigned) * p->scan_tmp_elems));
     return NFFT2D_OK;
 }
 
+
+// Self-test of the bounded device-side wait: one thread waits on an
+// mbarrier phase that nothing completes, gives up after `limit` polls (the
+// same mbar_wait_bounded the tiled kernels use) and records the timeout.
+__device__ int g_selftest_status;
+__global__ void k_selftest_wait(uint32_t limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_proxy_async_smem();
+        g_selftest_status = mbar_wait_bounded(&bar, 0, limit) ? 0 : kErrTimeout;
+    }
+}
 
 // Launch shape for the small elementwise kernels.
 dim3 row_grid(int cols, int rows) {
@@ -877,6 +917,20 @@ const char *nfft2d_status_string(int s) {
     }
 }
 
+int nfft2d_selftest_wait_timeout(int spin_limit, void *stream) {
+    if (spin_limit < 1) return NFFT2D_ERR_INVALID_ARG;
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int init = -1;
+    NFFT_TRY_CUDA(cudaMemcpyToSymbolAsync(g_selftest_status, &init, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+    k_selftest_wait<<<1, 32, 0, st>>>(static_cast<uint32_t>(spin_limit));
+    NFFT_TRY_CUDA(cudaGetLastError());
+    int h = -1;
+    NFFT_TRY_CUDA(cudaMemcpyFromSymbolAsync(&h, g_selftest_status, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+    NFFT_TRY_CUDA(cudaStreamSynchronize(st));
+    if (h == kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
+    return h == 0 ? NFFT2D_OK : NFFT2D_ERR_INTERNAL;
+}
+
 int nfft2d_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
@@ -956,9 +1010,9 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     cudaError_t e;
     if ((st = setup_grid(p)) != NFFT2D_OK) return fail(st);
     if ((st = setup_bins(p)) != NFFT2D_OK) return fail(st);
-    if ((e = cudaMalloc(&p->deap1, rs * N1)) != cudaSuccess) return fail(status_from_cuda(e));
-    if ((e = cudaMalloc(&p->deap2, rs * N2)) != cudaSuccess) return fail(status_from_cuda(e));
-    if ((e = cudaMalloc(&p->d_status, 4 * sizeof(int))) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = plan_malloc(reinterpret_cast<void **>(&p->deap1), rs * N1)) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = plan_malloc(reinterpret_cast<void **>(&p->deap2), rs * N2)) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = plan_malloc(reinterpret_cast<void **>(&p->d_status), 4 * sizeof(int))) != cudaSuccess) return fail(status_from_cuda(e));
     if ((e = cudaMemsetAsync(p->d_status, 0, 4 * sizeof(int), p->stream)) != cudaSuccess)
         return fail(status_from_cuda(e));
 

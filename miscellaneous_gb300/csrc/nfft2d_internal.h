@@ -78,6 +78,7 @@ struct Timer {
     bool on = false;
     cudaEvent_t ev[2 * kStages] = {};
     bool used[kStages] = {};
+    uint64_t nvtx[kStages] = {};  // open NVTX range of each stage (host-side trace)
 };
 
 }  // namespace nfft2d

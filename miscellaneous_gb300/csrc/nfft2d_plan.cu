@@ -9,6 +9,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -167,12 +168,20 @@ size_t rec_size(int precision) { return precision == NFFT2D_F64 ? sizeof(Rec64) 
 enum Stage { ST_SORT = 0, ST_PAD, ST_FFT2, ST_FILL, ST_GATHER, ST_SPREAD, ST_FOLD, ST_FFT1, ST_CROP, ST_COUNT };
 static_assert(ST_COUNT == kStages, "stage count");
 
+// Every stage is also an NVTX range on the host thread that enqueues it
+// (nfft2d:<stage>), so a system trace shows the library's calls; without a
+// tool attached the NVTX calls do nothing.
+const char *const kStageNames[ST_COUNT] = {"nfft2d:sort", "nfft2d:pad", "nfft2d:fft_type2", "nfft2d:halo_fill",
+                                           "nfft2d:gather", "nfft2d:spread", "nfft2d:fold", "nfft2d:fft_type1",
+                                           "nfft2d:crop"};
 void stage_begin(nfft2d_plan_s *p, Stage s) {
+    p->timer.nvtx[s] = nvtxRangeStartA(kStageNames[s]);
     if (!p->timer.on) return;
     cudaEventRecord(p->timer.ev[2 * s], p->stream);
     p->timer.used[s] = true;
 }
 void stage_end(nfft2d_plan_s *p, Stage s) {
+    nvtxRangeEnd(p->timer.nvtx[s]);
     if (!p->timer.on) return;
     cudaEventRecord(p->timer.ev[2 * s + 1], p->stream);
 }

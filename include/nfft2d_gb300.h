@@ -196,8 +196,9 @@ int nfft2d_ndft2d_f64(const double *X, const double *Y, const double *u, const d
  * particle in a host loop (Synthesis/PSO/PSO.cu:348, Synthesis.cu:395).
  * A batch holds `count` FP32 transforms (N1[t] x N2[t], shared sigma and K,
  * 16 x 16 tiles).  Grids of equal size share one batched cuFFT plan; every
- * other stage covers all transforms with one launch (persistent gather and
- * spread kernels over the work items of all transforms); the stage sequence
+ * other stage covers all transforms with one launch (a gather with one
+ * thread per binned point of all transforms, a persistent spread over the
+ * work items of all transforms); the stage sequence
  * is captured into a CUDA graph on first use and replayed (set_graph(0) runs
  * it eagerly instead).  set_points binds per-transform point arrays (FP32 or
  * FP64 coordinates, as nfft2d_set_points) and synchronizes; forward/adjoint

@@ -4,10 +4,11 @@
 // but every padded grid lives in ONE allocation, grouped by size, so the
 // FFTs of a size group run as one batched cuFFT call.  Each stage then covers
 // all transforms with a single launch: deapodize + pad, halo fill / fold and
-// crop walk (transform, row) pairs; the gather is a persistent kernel over
-// the concatenated work items of all transforms (TMA-staged patches); the
-// spread is a persistent warp kernel over the same items (register-resident
-// patches, one TMA reduce-add per item).  Per-transform descriptors -- the
+// crop walk (transform, row) pairs; the gather runs one thread per binned
+// point of all transforms (the transform found by the point's global index,
+// taps read straight from its grid, as the single-plan direct gather); the
+// spread is a persistent warp kernel over the concatenated work items of all
+// transforms (register-resident patches, one TMA reduce-add per item).  Per-transform descriptors -- the
 // TMA tensor map, geometry, record and work-item pointers -- sit in device
 // memory; the per-call input/output pointers go to a small device table
 // copied before each run.  The stage sequence is captured once into a CUDA
@@ -53,7 +54,7 @@ struct alignas(128) BatchDesc {
     int row_base;       // first global oversampled row (pad / halo kernels)
     int crop_base;      // first global output row (crop)
     int chunk;          // maximum points per work item
-    int pad_;
+    int point_base;     // first global point of this transform (direct gather)
 };
 
 struct BatchIO {
@@ -67,8 +68,10 @@ __device__ __forceinline__ int find_transform(const BatchDesc *__restrict__ d, i
     int lo = 0, hi = n - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        const int b = FIELD == 0 ? __ldg(&d[mid].chunk_base) : FIELD == 1 ? __ldg(&d[mid].row_base)
-                                                                           : __ldg(&d[mid].crop_base);
+        const int b = FIELD == 0   ? __ldg(&d[mid].chunk_base)
+                      : FIELD == 1 ? __ldg(&d[mid].row_base)
+                      : FIELD == 2 ? __ldg(&d[mid].crop_base)
+                                   : __ldg(&d[mid].point_base);
         if (b <= key)
             lo = mid;
         else
@@ -188,80 +191,27 @@ __global__ void k_batch_fold(const BatchDesc *__restrict__ d) {
     }
 }
 
-// ---- persistent gather over the work items of all transforms --------------
+// ---- gather over the points of all transforms --------------------------
+// Direct gather over all transforms: one thread per binned point, the
+// transform found by its global point index; taps read straight from that
+// transform's padded grid (the single-plan FP32 direct gather).
 template <int K>
-__device__ __forceinline__ void batch_issue(const BatchDesc *__restrict__ d, int n, int gc, float2 *dst,
-                                            uint64_t *bar) {
-    const int t = find_transform<0>(d, n, gc);
+__global__ void __launch_bounds__(kThreads)
+    k_batch_gather_direct(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total_points,
+                          const __grid_constant__ WinPoly wp, int *status) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= total_points) return;
+    const int t = find_transform<3>(d, n, i);
     const BatchDesc &D = d[t];
-    const int tile = __ldg(&D.chunks[gc - D.chunk_base].x);
-    const int tr = tile / D.g.tiles2, tc = tile - tr * D.g.tiles2;
-    mbar_arrive_expect_tx(bar, static_cast<uint32_t>(D.g.PR * D.g.PC * sizeof(float2)));
-    tma_load_2d(dst, &D.tmap, bar, 2 * (D.g.H + tc * D.g.T - D.g.Ke), D.g.H + tr * D.g.T - K);
-}
-
-template <int K, bool COMP>
-__global__ void __launch_bounds__(kThreads, 4)
-    k_batch_gather(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total, Geom g0,
-                   const __grid_constant__ WinPoly wp, int *status) {
-    extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_ok;
-    const int pstride = patch_stride_elems(g0);  // the same for every transform (same T, K)
-    float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_proxy_async_smem();
+    const int4 raw = __ldg(reinterpret_cast<const int4 *>(D.recs) + (i - D.point_base));
+    const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
+    const int n1 = __ldg(&D.g.n1), n2 = __ldg(&D.g.n2);
+    if (mu1 >= n1 || mu2 >= n2) {
+        latch_error(status, kErrBounds);
+        return;
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) < total) batch_issue<K>(d, n, blockIdx.x, bufs, &bars[0]);
-    uint32_t phase = 0;
-    int it = 0;
-    for (int gc = blockIdx.x; gc < total; gc += gridDim.x, ++it) {
-        const int b = it & 1;
-        const uint32_t par = (phase >> b) & 1u;
-        const int gnext = gc + gridDim.x;
-        if (threadIdx.x == 0) {
-            if (gnext < total) {
-                fence_proxy_async_smem();
-                batch_issue<K>(d, n, gnext, bufs + (b ^ 1) * pstride, &bars[b ^ 1]);
-            }
-            s_ok = mbar_wait_bounded(&bars[b], par) ? 1 : 0;
-        }
-        __syncthreads();
-        if (!s_ok) {
-            if (threadIdx.x == 0) {
-                latch_error(status, kErrTimeout);
-                if (gnext < total) (void)mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
-            }
-            return;
-        }
-        if (threadIdx.x != 0) (void)mbar_wait_bounded(&bars[b], par);
-        phase ^= (1u << b);
-
-        const int t = find_transform<0>(d, n, gc);
-        const BatchDesc &D = d[t];
-        const int4 ch = __ldg(&D.chunks[gc - D.chunk_base]);
-        const int tr = ch.x / D.g.tiles2, tc = ch.x - tr * D.g.tiles2;
-        const int r0 = tr * g0.T, c0 = tc * g0.T;
-        const float2 *patch = bufs + b * pstride;
-        const Rec32 *recs = D.recs;
-        float2 *out = io[t].out;
-        for (int i = threadIdx.x; i < ch.z; i += kThreads) {
-            const int4 raw = __ldg(reinterpret_cast<const int4 *>(recs) + ch.y + i);
-            const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
-            const int lr = mu1 - r0, lc = mu2 - c0;
-            if (static_cast<unsigned>(lr) >= static_cast<unsigned>(g0.T) ||
-                static_cast<unsigned>(lc) >= static_cast<unsigned>(g0.T)) {
-                latch_error(status, kErrBounds);
-                continue;
-            }
-            out[raw.w] = gather_point<K, COMP>(patch, g0.PC, g0.Ke, lr, lc, __int_as_float(raw.x),
-                                               __int_as_float(raw.y), wp);
-        }
-        __syncthreads();
-    }
+    io[t].out[raw.w] = gather_direct_f32<K>(D.grid, __ldg(&D.g.H), __ldg(&D.g.C), mu1, mu2, __int_as_float(raw.x),
+                                            __int_as_float(raw.y), wp);
 }
 
 // ---- persistent spread over the work items of all transforms --------------
@@ -330,7 +280,7 @@ struct nfft2d_batch_s {
     BatchIO *h_io = nullptr;  // pinned
     int *d_work = nullptr;    // spread work counter
     int *d_status = nullptr;  // [1] error bits (shared by the batched kernels)
-    int total_chunks = 0, total_rows = 0, total_crop = 0;
+    int total_chunks = 0, total_rows = 0, total_crop = 0, total_points = 0;
     bool points_valid = false;
     bool use_graph = true;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // type-2 forward, type-1 adjoint, type-1 sign -1
@@ -407,14 +357,9 @@ int enqueue_stages(nfft2d_batch_s *b, int type) {
         if (st != NFFT2D_OK) return st;
         k_batch_fill<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
         B_TRY(cudaGetLastError());
-        if (b->total_chunks > 0) {
-            const int smem = 2 * pstride * static_cast<int>(sizeof(float2)) + 128;
-            auto kernel = k_batch_gather<K, true>;
-            if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-            B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem));
-            const int blocks = std::max(1, std::min(b->total_chunks, std::max(per_sm, 1) * sms));
-            kernel<<<blocks, kThreads, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0, b->poly,
-                                                          b->d_status);
+        if (b->total_points > 0) {
+            k_batch_gather_direct<K><<<(b->total_points + kThreads - 1) / kThreads, kThreads, 0, b->stream>>>(
+                b->d_desc, n, b->d_io, b->total_points, b->poly, b->d_status);
             B_TRY(cudaGetLastError());
         }
     } else {
@@ -551,8 +496,10 @@ int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *
         b->groups.push_back(gr);
     }
     b->grid_bytes = elems * sizeof(float2);
-    if (cudaMalloc(&b->grids, b->grid_bytes) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
-    if (cudaMemsetAsync(b->grids, 0, b->grid_bytes, b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    // 256 zeroed bytes of slack after the last grid: the direct gather may
+    // read one complex past a grid's last row (with weight 0)
+    if (cudaMalloc(&b->grids, b->grid_bytes + 256) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (cudaMemsetAsync(b->grids, 0, b->grid_bytes + 256, b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     b->plans.assign(count, nullptr);
     for (int t = 0; t < count; ++t) {
         const int st = create_plan(&b->plans[t], N1[t], N2[t], sigma, K, NFFT2D_F32, kRegTile, b->stream,
@@ -596,6 +543,7 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
     B_TRY(cudaStreamSynchronize(b->stream));
     std::vector<BatchDesc> h(b->count);
     int chunks = 0, rows = 0, crop = 0;
+    long long points = 0;
     for (int t = 0; t < b->count; ++t) {
         nfft2d_plan_s *p = b->plans[t];
         const int st = nfft2d_set_points(p, M[t], x1[t], x2[t], coord_dtype, units);
@@ -616,12 +564,16 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
         D.row_base = rows;
         D.crop_base = crop;
         D.chunk = p->chunk;
+        D.point_base = static_cast<int>(points);
+        points += p->M;
         chunks += D.n_chunks;
         rows += p->g.n1;
         crop += p->N1;
     }
     B_TRY(cudaMemcpy(b->d_desc, h.data(), sizeof(BatchDesc) * b->count, cudaMemcpyHostToDevice));
+    if (points > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;  // global point indices are int
     b->total_chunks = chunks;
+    b->total_points = static_cast<int>(points);
     b->total_rows = rows;
     b->total_crop = crop;
     b->points_valid = true;

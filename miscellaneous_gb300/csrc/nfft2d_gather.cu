@@ -194,44 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
     weights_any<K, Real>(static_cast<Real>(r.t1), w1, a);
     weights_any<K, Real>(static_cast<Real>(r.t2), w2, a);
     if constexpr (MODE == 0 && sizeof(Real) == 4) {
-        // 16-byte loads, two taps each: a row's 2K+1 taps start at an even or
-        // odd complex column; read the 2K+2 columns from the 16-byte boundary
-        // at or below it and shift the column weights by one for odd starts
-        // (the extra column gets weight 0; it lies inside the padded grid, or
-        // in the zeroed slack after it).
-        constexpr int V = K + 1;  // float4 loads per row
-        const int col0 = mu2 + g.H - K;
-        const int odd = col0 & 1;
-        float ws[2 * V];
-#pragma unroll
-        for (int q = 0; q < 2 * V; ++q) {
-            const float lo = q < W ? w2[q] : 0.f;
-            const float hi = (q >= 1 && q - 1 < W) ? w2[q - 1] : 0.f;
-            ws[q] = odd ? hi : lo;
-        }
-        const float4 *rb = reinterpret_cast<const float4 *>(grid + static_cast<size_t>(mu1 + g.H - K) * g.C +
-                                                            (col0 - odd));
-        const int pitch4 = g.C >> 1;
-        float sx = 0.f, sy = 0.f;
-#pragma unroll
-        for (int rr = 0; rr < W; ++rr) {
-            const float4 *row = rb + rr * pitch4;
-            float rx = 0.f, ry = 0.f;
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-                const float4 v = __ldg(row + q);
-                rx = fmaf(ws[2 * q], v.x, rx);
-                ry = fmaf(ws[2 * q], v.y, ry);
-                rx = fmaf(ws[2 * q + 1], v.z, rx);
-                ry = fmaf(ws[2 * q + 1], v.w, ry);
-            }
-            sx = fmaf(w1[rr], rx, sx);
-            sy = fmaf(w1[rr], ry, sy);
-        }
-        Cx o;
-        o.x = sx;
-        o.y = sy;
-        out[r.orig] = o;
+        out[r.orig] = gather_direct_f32<K>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
     } else if (MODE == 0) {
         Real sx = 0, sy = 0;
 #pragma unroll

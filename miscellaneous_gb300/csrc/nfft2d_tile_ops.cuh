@@ -53,6 +53,53 @@ __device__ __forceinline__ float2 gather_point(const float2 *__restrict__ patch,
 }
 
 // ---------------------------------------------------------------------------
+// gather: one point straight from the padded grid (L1/L2), FP32
+// ---------------------------------------------------------------------------
+
+// 16-byte loads, two taps each: a row's 2K+1 taps start at an even or odd
+// complex column; the 2K+2 columns from the 16-byte boundary at or below it
+// are read and the column weights shifted by one for odd starts (the extra
+// column gets weight 0; it lies inside the padded grid, or in the zeroed
+// slack after it).  Grid rows start on 16-byte boundaries (even pitch).
+template <int K>
+__device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ grid, int H, int C, int mu1, int mu2,
+                                                    float t1, float t2, const WinPoly &wp) {
+    constexpr int W = 2 * K + 1;
+    constexpr int V = K + 1;  // float4 loads per row
+    float w1[W], w2[W];
+    weights_poly<K>(t1, w1, wp);
+    weights_poly<K>(t2, w2, wp);
+    const int col0 = mu2 + H - K;
+    const int odd = col0 & 1;
+    float ws[2 * V];
+#pragma unroll
+    for (int q = 0; q < 2 * V; ++q) {
+        const float lo = q < W ? w2[q] : 0.f;
+        const float hi = (q >= 1 && q - 1 < W) ? w2[q - 1] : 0.f;
+        ws[q] = odd ? hi : lo;
+    }
+    const float4 *rb = reinterpret_cast<const float4 *>(grid + static_cast<size_t>(mu1 + H - K) * C + (col0 - odd));
+    const int pitch4 = C >> 1;
+    float sx = 0.f, sy = 0.f;
+#pragma unroll
+    for (int rr = 0; rr < W; ++rr) {
+        const float4 *row = rb + rr * pitch4;
+        float rx = 0.f, ry = 0.f;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            const float4 v = __ldg(row + q);
+            rx = fmaf(ws[2 * q], v.x, rx);
+            ry = fmaf(ws[2 * q], v.y, ry);
+            rx = fmaf(ws[2 * q + 1], v.z, rx);
+            ry = fmaf(ws[2 * q + 1], v.w, ry);
+        }
+        sx = fmaf(w1[rr], rx, sx);
+        sy = fmaf(w1[rr], ry, sy);
+    }
+    return make_float2(sx, sy);
+}
+
+// ---------------------------------------------------------------------------
 // spread: a warp accumulates a 16 x 16 tile's (16+2K) x 32 patch in registers
 // ---------------------------------------------------------------------------
 constexpr int kRegTile = 16;  // tile edge the register-resident spread requires

@@ -4,7 +4,8 @@
  * One shared library, libnfft2d_gb300.so, exports every function declared
  * here with C linkage: plain pointers, sizes and status codes, no C++ or
  * torch types.  Array arguments are DEVICE pointers owned by the caller
- * (as in the reference, NFFT/NFFT2_2D.cuh:8-11 and NFFT/NDFT2_2D.cuh:4-6);
+ * (as in the reference, NFFT/NFFT2_2D.cuh:8-11 and NFFT/NDFT2_2D.cuh:4-6;
+ * nfft2d_set_points also takes page-locked host coordinates);
  * work buffers are owned by a plan, allocated once at plan creation /
  * set_points, never per call.
  *
@@ -145,7 +146,10 @@ int nfft2d_layout_query(int N1, int N2, double sigma, int K, int precision, int 
  * reference recomputes mu = rint(c*x) per call inside
  * Interpolation_NFFT2_2D_GPUKernel, NFFT2_2D.cu:163-173).  The coordinate
  * reduction runs in FP64.  Synchronizes the plan's stream.  M = 0 is valid
- * (transforms then produce zeros). */
+ * (transforms then produce zeros).  x1, x2 may be device memory or
+ * page-locked host memory (read over the host link by the binning pass
+ * itself, no separate upload); other host memory only where the device can
+ * read pageable memory, else NFFT2D_ERR_INVALID_ARG. */
 int nfft2d_set_points(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype, int units);
 
 /* ---- transforms ---------------------------------------------------------

@@ -105,7 +105,6 @@ struct nfft2d_plan_s {
     int *d_status = nullptr;     // [0] n_chunks, [1] error bits
     unsigned *cell_count = nullptr;  // ncells + 1 counters / starts
     size_t ncells = 0;
-    unsigned *tile_chunks = nullptr; // ntiles + 1
     unsigned *scan_tmp = nullptr;
     size_t scan_tmp_elems = 0;
 

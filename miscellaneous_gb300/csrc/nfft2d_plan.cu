@@ -434,8 +434,11 @@ template <typename CT, typename RecT>
 __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double o1, double o2,
                             double s1, double s2, float s1f, float s2f, int exact_f32, Geom g, RecT *__restrict__ tmp,
                             unsigned *__restrict__ ranks, unsigned *__restrict__ cell_count,
-                            int *__restrict__ status) {
+                            int *__restrict__ status, unsigned long long *__restrict__ scan_state,
+                            int scan_words) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // the two scans that follow start from zeroed tickets and tile words
+    for (int k = i; k < scan_words; k += gridDim.x * blockDim.x) scan_state[k] = 0ull;
     if (i >= M) return;
     RecT r;
     int mu1, mu2;
@@ -467,73 +470,69 @@ __global__ void k_bin_scatter(const RecT *__restrict__ tmp, const unsigned *__re
     recs[cell_start[key] + ranks[i]] = r;
 }
 
-__global__ void k_tile_chunk_count(const unsigned *__restrict__ cell_start, int ntiles, int cells_per_tile, int chunk,
-                                   unsigned *__restrict__ tile_chunks) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t > ntiles) return;
-    if (t == ntiles) {
-        tile_chunks[t] = 0;
-        return;
-    }
-    const unsigned a = cell_start[static_cast<size_t>(t) * cells_per_tile];
-    const unsigned b = cell_start[static_cast<size_t>(t + 1) * cells_per_tile];
-    tile_chunks[t] = (b - a + chunk - 1) / chunk;
-}
-
-__global__ void k_emit_chunks(const unsigned *__restrict__ cell_start, const unsigned *__restrict__ tile_chunks,
-                              int ntiles, int cells_per_tile, int chunk, int4 *__restrict__ chunks,
-                              int *__restrict__ status) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles) return;
-    if (t == 0) status[0] = static_cast<int>(tile_chunks[ntiles]);
-    const unsigned base = tile_chunks[t];
-    const unsigned nch = tile_chunks[t + 1] - base;
-    const unsigned start = cell_start[static_cast<size_t>(t) * cells_per_tile];
-    const unsigned cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] - start;
-    for (unsigned c = 0; c < nch; ++c) {
-        const unsigned off = c * chunk;
-        chunks[base + c] = make_int4(t, static_cast<int>(start + off), static_cast<int>(min(cnt - off, (unsigned)chunk)), 0);
-    }
-}
-
 // ---------------------------------------------------------------------------
-// exclusive scan of unsigned counters (3 phases, recursive on block sums)
+// single-pass exclusive scans (decoupled look-back)
 // ---------------------------------------------------------------------------
+// Blocks take tiles of kScanTile consecutive counters in launch order from a
+// ticket counter, scan them locally, publish the tile's aggregate, then walk
+// back over the predecessors' published words until one carries its
+// inclusive prefix.  A tile only waits on tiles whose blocks took earlier
+// tickets (already running), and every wait is bounded: a block that gives up
+// latches kErrTimeout and treats the missing value as 0, so the host sees an
+// error status instead of a hang.  One launch replaces the three-phase
+// reduce / scan-of-sums / apply sequence.
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr unsigned long long kTileAggregate = 1ull << 32;
+constexpr unsigned long long kTilePrefix = 2ull << 32;
 
-__global__ void k_scan_reduce(const unsigned *__restrict__ in, size_t n, unsigned *__restrict__ sums) {
-    __shared__ unsigned warp_sums[kScanThreads / 32];
-    const size_t base = static_cast<size_t>(blockIdx.x) * kScanTile;
-    unsigned s = 0;
-    for (int k = 0; k < kScanItems; ++k) {
-        const size_t i = base + static_cast<size_t>(k) * kScanThreads + threadIdx.x;
-        if (i < n) s += in[i];
+// Scan state for one scan over n counters: a ticket counter (as a 64-bit
+// word) followed by one status word per tile.
+size_t scan_state_words(size_t n) { return 1 + (n + kScanTile - 1) / kScanTile; }
+
+// The block's exclusive offset of this tile among all tiles; `agg` is the
+// tile's own sum.  Called by thread 0 only.
+__device__ unsigned tile_lookback(unsigned long long *tile_word, int tile, unsigned agg, int *status) {
+    if (tile == 0) {
+        atomicExch(tile_word, kTilePrefix | agg);
+        return 0u;
     }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        unsigned v = threadIdx.x < kScanThreads / 32 ? warp_sums[threadIdx.x] : 0u;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) sums[blockIdx.x] = v;
+    atomicExch(tile_word + tile, kTileAggregate | agg);
+    unsigned excl = 0;
+    for (int j = tile - 1; j >= 0; --j) {
+        unsigned long long w = 0;
+        uint32_t spins = 0;
+        for (;;) {
+            w = *reinterpret_cast<volatile unsigned long long *>(tile_word + j);
+            if (w >> 32) break;
+            if (++spins >= kSpinLimit) break;
+            if (spins > 16) __nanosleep(64);
+        }
+        if (!(w >> 32)) {
+            latch_error(status, kErrTimeout);
+            break;
+        }
+        excl += static_cast<unsigned>(w);
+        if ((w >> 32) == (kTilePrefix >> 32)) break;
     }
+    atomicExch(tile_word + tile, kTilePrefix | (excl + agg));
+    return excl;
 }
 
-__global__ void k_scan_apply(unsigned *__restrict__ data, size_t n, const unsigned *__restrict__ offsets) {
+// Exclusive scan of the block's kScanTile items (v: the thread's
+// kScanItems consecutive values) across all tiles: returns the exclusive
+// prefix of the thread's first item.  `state` is the scan's ticket + words.
+__device__ unsigned block_scan_lookback(const unsigned (&v)[kScanItems], int tile, unsigned long long *state,
+                                        int *status) {
     __shared__ unsigned warp_tot[kScanThreads / 32];
-    const size_t base = static_cast<size_t>(blockIdx.x) * kScanTile + static_cast<size_t>(threadIdx.x) * kScanItems;
-    unsigned v[kScanItems];
+    __shared__ unsigned block_agg, block_excl;
     unsigned tsum = 0;
-    for (int k = 0; k < kScanItems; ++k) {
-        const size_t i = base + k;
-        v[k] = i < n ? data[i] : 0u;
-        tsum += v[k];
-    }
-    // block-wide exclusive scan of thread totals
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) tsum += v[k];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned incl = tsum;
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
@@ -541,44 +540,97 @@ __global__ void k_scan_apply(unsigned *__restrict__ data, size_t n, const unsign
     if (lane == 31) warp_tot[wid] = incl;
     __syncthreads();
     if (wid == 0) {
-        unsigned w = lane < kScanThreads / 32 ? warp_tot[lane] : 0u;
+        const unsigned w = lane < kScanThreads / 32 ? warp_tot[lane] : 0u;
         unsigned wi = w;
+#pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
             if (lane >= o) wi += y;
         }
         if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
+        if (lane == 31) block_agg = wi;
     }
     __syncthreads();
-    unsigned run = (offsets ? offsets[blockIdx.x] : 0u) + warp_tot[wid] + (incl - tsum);
+    if (threadIdx.x == 0) block_excl = tile_lookback(state + 1, tile, block_agg, status);
+    __syncthreads();
+    return block_excl + warp_tot[wid] + (incl - tsum);
+}
+
+__device__ __forceinline__ int scan_ticket(unsigned long long *state) {
+    __shared__ int t;
+    if (threadIdx.x == 0) t = static_cast<int>(atomicAdd(state, 1ull));
+    __syncthreads();
+    return t;
+}
+
+// In-place exclusive scan of n counters.
+__global__ void __launch_bounds__(kScanThreads) k_scan_counts(unsigned *__restrict__ data, size_t n,
+                                                              unsigned long long *state, int *status) {
+    const int tile = scan_ticket(state);
+    const size_t base = static_cast<size_t>(tile) * kScanTile + static_cast<size_t>(threadIdx.x) * kScanItems;
+    unsigned v[kScanItems];
+    if (base + kScanItems <= n) {
+        const uint4 a = *reinterpret_cast<const uint4 *>(data + base);
+        const uint4 b = *reinterpret_cast<const uint4 *>(data + base + 4);
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? data[base + k] : 0u;
+    }
+    unsigned run = block_scan_lookback(v, tile, state, status);
+    if (base + kScanItems <= n) {
+        uint4 a, b;
+        a.x = run, run += v[0], a.y = run, run += v[1], a.z = run, run += v[2], a.w = run, run += v[3];
+        b.x = run, run += v[4], b.y = run, run += v[5], b.z = run, run += v[6], b.w = run;
+        *reinterpret_cast<uint4 *>(data + base) = a;
+        *reinterpret_cast<uint4 *>(data + base + 4) = b;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n) {
+                data[base + k] = run;
+                run += v[k];
+            }
+    }
+}
+
+// Work items from the scanned cell starts: tile t (cells_per_tile cells from
+// t * cells_per_tile) holds ceil(count / chunk) items of up to `chunk`
+// points.  One scan over the per-tile item counts places every tile's items;
+// the thread owning index ntiles stores the total in status[0].
+__global__ void __launch_bounds__(kScanThreads, 1) k_scan_emit_chunks(const unsigned *__restrict__ cell_start, int ntiles,
+                                                                   int cells_per_tile, int chunk,
+                                                                   int4 *__restrict__ chunks,
+                                                                   unsigned long long *state, int *status) {
+    const int tile = scan_ticket(state);
+    const long long base = static_cast<long long>(tile) * kScanTile + static_cast<long long>(threadIdx.x) * kScanItems;
+    unsigned v[kScanItems];
+#pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-        const size_t i = base + k;
-        if (i < n) data[i] = run;
+        const long long t = base + k;
+        v[k] = 0u;
+        if (t < ntiles) {
+            const unsigned cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] -
+                                 cell_start[static_cast<size_t>(t) * cells_per_tile];
+            v[k] = (cnt + chunk - 1) / chunk;
+        }
+    }
+    unsigned run = block_scan_lookback(v, tile, state, status);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const long long t = base + k;
+        if (t == ntiles) status[0] = static_cast<int>(run);
+        if (v[k]) {
+            const unsigned start = cell_start[static_cast<size_t>(t) * cells_per_tile];
+            const unsigned cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] - start;
+            for (unsigned c = 0; c < v[k]; ++c) {
+                const unsigned off = c * chunk;
+                chunks[run + c] = make_int4(static_cast<int>(t), static_cast<int>(start + off),
+                                            static_cast<int>(min(cnt - off, static_cast<unsigned>(chunk))), 0);
+            }
+        }
         run += v[k];
     }
-}
-
-size_t scan_tmp_needed(size_t n) {
-    size_t total = 0;
-    while (n > static_cast<size_t>(kScanTile)) {
-        n = (n + kScanTile - 1) / kScanTile;
-        total += n;
-    }
-    return total + 64;
-}
-
-cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *tmp, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    const size_t nb = (n + kScanTile - 1) / kScanTile;
-    if (nb == 1) {
-        k_scan_apply<<<1, kScanThreads, 0, st>>>(data, n, nullptr);
-        return cudaGetLastError();
-    }
-    k_scan_reduce<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(data, n, tmp);
-    cudaError_t e = exclusive_scan(tmp, nb, tmp + nb, st);
-    if (e != cudaSuccess) return e;
-    k_scan_apply<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(data, n, tmp);
-    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -609,7 +661,6 @@ void destroy_plan(nfft2d_plan_s *p) {
     cudaFree(p->deap2);
     cudaFree(p->d_status);
     cudaFree(p->cell_count);
-    cudaFree(p->tile_chunks);
     cudaFree(p->scan_tmp);
     for (auto &e : p->timer.ev)
         if (e) cudaEventDestroy(e);
@@ -640,7 +691,7 @@ size_t plan_workspace_bytes(const nfft2d_plan_s *p) {
     const size_t grid = cplx_size(p->precision) * static_cast<size_t>(p->g.Ra) * p->g.C;
     const size_t pts = static_cast<size_t>(p->capM) * (2 * rec_size(p->precision) + sizeof(unsigned)) +
                        static_cast<size_t>(p->chunks_cap) * sizeof(int4);
-    const size_t bins = sizeof(unsigned) * (p->ncells + 1 + p->g.tiles1 * p->g.tiles2 + 1 + p->scan_tmp_elems);
+    const size_t bins = sizeof(unsigned) * (p->ncells + 1 + p->scan_tmp_elems);
     return grid + pts + bins + real_size(p->precision) * (p->N1 + p->N2);
 }
 
@@ -702,14 +753,13 @@ int setup_grid(nfft2d_plan_s *p) {
 int setup_bins(nfft2d_plan_s *p) {
     const Geom &g = p->g;
     cudaFree(p->cell_count);
-    cudaFree(p->tile_chunks);
     cudaFree(p->scan_tmp);
-    p->cell_count = p->tile_chunks = p->scan_tmp = nullptr;
+    p->cell_count = p->scan_tmp = nullptr;
     p->ncells = static_cast<size_t>(g.tiles1) * g.tiles2 * g.T * g.T;
-    const int ntiles = g.tiles1 * g.tiles2;
-    p->scan_tmp_elems = std::max(scan_tmp_needed(p->ncells + 1), scan_tmp_needed(ntiles + 1));
+    const size_t ntiles = static_cast<size_t>(g.tiles1) * g.tiles2;
+    // two 64-bit scan states (cells, work items), counted in 32-bit words
+    p->scan_tmp_elems = 2 * (scan_state_words(p->ncells + 1) + scan_state_words(ntiles + 1));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->cell_count), sizeof(unsigned) * (p->ncells + 1)));
-    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->tile_chunks), sizeof(unsigned) * (ntiles + 1)));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->scan_tmp), sizeof(unsigned) * p->scan_tmp_elems));
     return NFFT2D_OK;
 }
@@ -1159,6 +1209,35 @@ static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, co
     return nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0);
 }
 
+// The address the binning kernel reads coordinates through: device or
+// managed memory as given; page-locked host memory (cudaHostAlloc,
+// cudaHostRegister) through its device mapping, so the binning pass itself
+// pulls the coordinates over the host link and no separate upload runs
+// first; other host memory only where the device can read pageable memory
+// (cudaDevAttrPageableMemoryAccess, e.g. a coherent CPU-GPU link), else
+// INVALID_ARG instead of a faulting read.
+static int coord_device_ptr(const nfft2d_plan_s *p, const void *x, const void **dx) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, x) != cudaSuccess) {
+        cudaGetLastError();
+        return NFFT2D_ERR_INVALID_ARG;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+        *dx = x;
+        return NFFT2D_OK;
+    }
+    if (a.type == cudaMemoryTypeHost) {
+        if (!a.devicePointer) return NFFT2D_ERR_INVALID_ARG;
+        *dx = a.devicePointer;
+        return NFFT2D_OK;
+    }
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p->device) != cudaSuccess || !pageable)
+        return NFFT2D_ERR_INVALID_ARG;
+    *dx = x;
+    return NFFT2D_OK;
+}
+
 extern "C++" {
 int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype,
                               double u1, double u2, double o1, double o2) {
@@ -1169,6 +1248,11 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
         !std::isfinite(o2))
         return NFFT2D_ERR_INVALID_ARG;
     if (M > 0 && (!x1 || !x2)) return NFFT2D_ERR_INVALID_ARG;
+    if (M > 0) {
+        int st = coord_device_ptr(p, x1, &x1);
+        if (st == NFFT2D_OK) st = coord_device_ptr(p, x2, &x2);
+        if (st != NFFT2D_OK) return st;
+    }
     p->points_valid = false;
     p->M = 0;
     p->n_chunks = 0;
@@ -1194,27 +1278,34 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     NFFT_TRY_CUDA(cudaMemsetAsync(p->cell_count, 0, sizeof(unsigned) * (p->ncells + 1), p->stream));
     const int Mi = static_cast<int>(M);
     const int blocks = (Mi + 255) / 256;
+    // ticket + tile words of the cell scan, then of the work-item scan
+    unsigned long long *scan_state = reinterpret_cast<unsigned long long *>(p->scan_tmp);
+    const int scan_words = static_cast<int>(scan_state_words(p->ncells + 1) +
+                                            scan_state_words(static_cast<size_t>(g.tiles1) * g.tiles2 + 1));
     if (p->precision == NFFT2D_F64) {
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec64><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
         else
             k_bin_pass1<float, Rec64><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
     } else {
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec32><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
         else
             k_bin_pass1<float, Rec32><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status);
+                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
     }
     NFFT_TRY_CUDA(cudaGetLastError());
-    NFFT_TRY_CUDA(exclusive_scan(p->cell_count, p->ncells + 1, p->scan_tmp, p->stream));
+    const size_t cells_n = p->ncells + 1;
+    k_scan_counts<<<static_cast<unsigned>((cells_n + kScanTile - 1) / kScanTile), kScanThreads, 0, p->stream>>>(
+        p->cell_count, cells_n, scan_state, p->d_status);
+    NFFT_TRY_CUDA(cudaGetLastError());
     if (p->precision == NFFT2D_F64)
         k_bin_scatter<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->tmp_recs), p->ranks,
                                                             p->cell_count, Mi, static_cast<Rec64 *>(p->recs));
@@ -1223,19 +1314,16 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
                                                             p->cell_count, Mi, static_cast<Rec32 *>(p->recs));
     NFFT_TRY_CUDA(cudaGetLastError());
     const int ntiles = g.tiles1 * g.tiles2;
-    const int cpt = g.T * g.T;
-    k_tile_chunk_count<<<(ntiles + 1 + 255) / 256, 256, 0, p->stream>>>(p->cell_count, ntiles, cpt, p->chunk,
-                                                                        p->tile_chunks);
-    NFFT_TRY_CUDA(cudaGetLastError());
-    NFFT_TRY_CUDA(exclusive_scan(p->tile_chunks, ntiles + 1, p->scan_tmp, p->stream));
-    k_emit_chunks<<<(ntiles + 255) / 256, 256, 0, p->stream>>>(p->cell_count, p->tile_chunks, ntiles, cpt, p->chunk,
-                                                               p->chunks, p->d_status);
+    k_scan_emit_chunks<<<static_cast<unsigned>((ntiles + 1 + kScanTile - 1) / kScanTile), kScanThreads, 0,
+                         p->stream>>>(p->cell_count, ntiles, g.T * g.T, p->chunk, p->chunks,
+                                      scan_state + scan_state_words(cells_n), p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
     stage_end(p, ST_SORT);
     int hs[4] = {0, 0, 0, 0};
     NFFT_TRY_CUDA(cudaMemcpyAsync(hs, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
     NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
     if (hs[1] & kErrNonfinite) return NFFT2D_ERR_NONFINITE;
+    if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
     if (hs[0] < 0 || hs[0] > p->chunks_cap) return NFFT2D_ERR_INTERNAL;
     p->n_chunks = hs[0];
     p->M = M;

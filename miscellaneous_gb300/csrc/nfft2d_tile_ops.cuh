@@ -80,23 +80,25 @@ __device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ g
     }
     const float4 *rb = reinterpret_cast<const float4 *>(grid + static_cast<size_t>(mu1 + H - K) * C + (col0 - odd));
     const int pitch4 = C >> 1;
-    float sx = 0.f, sy = 0.f;
+    // (re, im) of a cell times a real weight: one packed FP32x2 FMA, rounded
+    // as two fmaf (2-3 % faster than scalar FMAs on GB300 at K = 2..8).
+    float2 wsp[2 * V];
+#pragma unroll
+    for (int q = 0; q < 2 * V; ++q) wsp[q] = make_float2(ws[q], ws[q]);
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
     for (int rr = 0; rr < W; ++rr) {
         const float4 *row = rb + rr * pitch4;
-        float rx = 0.f, ry = 0.f;
+        float2 r = make_float2(0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < V; ++q) {
             const float4 v = __ldg(row + q);
-            rx = fmaf(ws[2 * q], v.x, rx);
-            ry = fmaf(ws[2 * q], v.y, ry);
-            rx = fmaf(ws[2 * q + 1], v.z, rx);
-            ry = fmaf(ws[2 * q + 1], v.w, ry);
+            r = __ffma2_rn(make_float2(v.x, v.y), wsp[2 * q], r);
+            r = __ffma2_rn(make_float2(v.z, v.w), wsp[2 * q + 1], r);
         }
-        sx = fmaf(w1[rr], rx, sx);
-        sy = fmaf(w1[rr], ry, sy);
+        s = __ffma2_rn(r, make_float2(w1[rr], w1[rr]), s);
     }
-    return make_float2(sx, sy);
+    return s;
 }
 
 // ---------------------------------------------------------------------------

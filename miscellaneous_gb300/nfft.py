@@ -130,8 +130,13 @@ class Plan:
             raise ValueError("x1 and x2 must be 1-D tensors of equal length")
         if x1.dtype not in (torch.float32, torch.float64) or x2.dtype != x1.dtype:
             raise TypeError("coordinates must both be float32 or both float64")
-        _require_cuda(x1, "x1", x1.dtype)
-        _require_cuda(x2, "x2", x1.dtype)
+        for t, name in ((x1, "x1"), (x2, "x2")):
+            if t.is_cuda:
+                _require_cuda(t, name, x1.dtype)
+            elif not (t.is_pinned() and t.is_contiguous()):
+                # page-locked host coordinates are read by the binning pass
+                # over the host link, with no separate upload
+                raise TypeError(f"{name} must be a CUDA tensor or a contiguous pinned CPU tensor")
         cd = _lib.COORD_F32 if x1.dtype == torch.float32 else _lib.COORD_F64
         M = x1.numel()
         check(self._lib.nfft2d_set_points(self._h, M, _ptr(x1), _ptr(x2), cd, _lib.UNITS[units]),

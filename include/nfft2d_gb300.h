@@ -152,6 +152,18 @@ int nfft2d_layout_query(int N1, int N2, double sigma, int K, int precision, int 
  * read pageable memory, else NFFT2D_ERR_INVALID_ARG. */
 int nfft2d_set_points(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype, int units);
 
+/* As nfft2d_set_points, but returns once the binning is enqueued on the
+ * plan's stream, without a host round trip (no reference counterpart: the
+ * reference re-derives the bins inside every transform).  The transforms
+ * that follow read the work-item count from device memory; x1 and x2 must
+ * stay valid until the stream has run the binning.  A non-finite coordinate
+ * is reported by the next nfft2d_synchronize (NFFT2D_ERR_NONFINITE, which
+ * also drops the point set); transforms enqueued before that produce
+ * unspecified values but stay in bounds.  nfft2d_get_info reports n_chunks
+ * = -1 until nfft2d_synchronize has read the count back. */
+int nfft2d_set_points_async(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype,
+                            int units);
+
 /* ---- transforms ---------------------------------------------------------
  * nfft2d_forward   : type 2, sign -1  (BP_FBP_FFBP/NFFT1_2D.m:1-69)
  * nfft2d_adjoint   : type 1, sign +1  (Hermitian adjoint of nfft2d_forward)

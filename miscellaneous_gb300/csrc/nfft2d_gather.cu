@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
     const int pstride = patch_stride_elems(g);
     // TMA shared-memory operands: 128-byte aligned (the launch adds 128 bytes of slack)
     float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    const int n = a.n_chunks;
+    const int n = a.n_chunks >= 0 ? a.n_chunks : a.status[0];  // < 0: counted on the device only
 
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
@@ -265,7 +265,7 @@ cudaError_t launch_K(const nfft2d_plan_s *p, void *f, const void *v, void *g1, v
         cudaError_t e = prepare_smem(kernel, smem);
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kThreads, smem);
-        if (blocks > p->n_chunks) blocks = static_cast<int>(p->n_chunks);
+        if (p->n_chunks >= 0 && blocks > p->n_chunks) blocks = static_cast<int>(p->n_chunks);
         kernel<<<blocks, kThreads, smem, p->stream>>>(p->tmap, static_cast<const Rec32 *>(p->recs), p->chunks,
                                                       static_cast<float2 *>(f), static_cast<const float2 *>(v),
                                                       static_cast<float *>(g1), static_cast<float *>(g2), a);

@@ -103,6 +103,7 @@ struct nfft2d_plan_s {
     void *deap1 = nullptr;       // N1 reals: S / phi(xi_k1), plan precision
     void *deap2 = nullptr;       // N2 reals
     int *d_status = nullptr;     // [0] n_chunks, [1] error bits
+    int *h_status = nullptr;     // page-locked host copy of d_status
     unsigned *cell_count = nullptr;  // ncells + 1 counters / starts
     size_t ncells = 0;
     unsigned *scan_tmp = nullptr;
@@ -165,9 +166,11 @@ void release_plan(nfft2d_plan_s *p);
 int tensor_map_for(nfft2d_plan_s *p);
 
 // Bin points whose grid-unit coordinates are (x - o) * u per dimension (the
-// public set_points uses o = 0 and u from its units argument).
+// public set_points uses o = 0 and u from its units argument).  async: return
+// after enqueuing; the work-item count stays on the device (n_chunks = -1)
+// until nfft2d_synchronize reads it back with the error bits.
 int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype, double u1,
-                      double u2, double o1, double o2);
+                      double u2, double o1, double o2, bool async = false);
 
 // A type-2 transform whose deapodized, zero-padded coefficients are written
 // into the grid interior by `pad` (launched on the plan's stream, timed as
@@ -176,9 +179,10 @@ int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void 
 typedef cudaError_t (*PadFn)(const nfft2d_plan_s *p, const void *ctx);
 int type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const void *ctx);
 
-// cudaMalloc for plan buffers, with the host-side allocation-failure hook
-// used by the tests (see nfft2d_plan.cu).
+// cudaMalloc / cudaMallocHost for plan buffers, with the host-side
+// allocation-failure hook used by the tests (NFFT2D_FAIL_ALLOC_AT).
 cudaError_t plan_malloc(void **ptr, size_t bytes);
+cudaError_t plan_malloc_host(void **ptr, size_t bytes);
 
 // Host FP64 helpers shared by the plan and the Knab regridder.
 double bessel_i0_host(double x);

@@ -112,23 +112,36 @@ double nfft2d::fit_window_poly(double sigma, int K, WinPoly *out) {
 // the variable takes that value) report cudaErrorMemoryAllocation without
 // allocating; unset, it is one getenv per allocation (plan creation and
 // set_points only, never per transform).
-cudaError_t nfft2d::plan_malloc(void **ptr, size_t bytes) {
+// NFFT2D_FAIL_ALLOC_AT=k: the k-th plan allocation (device or pinned host,
+// counted since the variable last changed) fails.
+static bool injected_alloc_failure() {
     static std::mutex mu;
     static std::string seen;
     static long long count = 0;
     const char *v = std::getenv("NFFT2D_FAIL_ALLOC_AT");
-    if (v && *v) {
-        std::lock_guard<std::mutex> lock(mu);
-        if (seen != v) {
-            seen = v;
-            count = 0;
-        }
-        if (++count == std::atoll(v)) {
-            *ptr = nullptr;
-            return cudaErrorMemoryAllocation;
-        }
+    if (!v || !*v) return false;
+    std::lock_guard<std::mutex> lock(mu);
+    if (seen != v) {
+        seen = v;
+        count = 0;
+    }
+    return ++count == std::atoll(v);
+}
+
+cudaError_t nfft2d::plan_malloc(void **ptr, size_t bytes) {
+    if (injected_alloc_failure()) {
+        *ptr = nullptr;
+        return cudaErrorMemoryAllocation;
     }
     return cudaMalloc(ptr, bytes);
+}
+
+cudaError_t nfft2d::plan_malloc_host(void **ptr, size_t bytes) {
+    if (injected_alloc_failure()) {
+        *ptr = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMallocHost(ptr, bytes);
 }
 
 namespace {
@@ -445,9 +458,12 @@ __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2
     const bool ok1 = reduce_coord(x1[i], o1, s1, s1f, exact_f32 != 0, g.n1, mu1, r.t1);
     const bool ok2 = reduce_coord(x2[i], o2, s2, s2f, exact_f32 != 0, g.n2, mu2, r.t2);
     if (!ok1 || !ok2) {
+        // the error is reported; the point is still binned (at cell 0, t = 0)
+        // so every sorted record stays in bounds for transforms that an
+        // asynchronous set_points lets run before the status is read
         latch_error(status, kErrNonfinite);
-        tmp[i].orig = static_cast<int>(kInvalidKey);
-        return;
+        mu1 = mu2 = 0;
+        r.t1 = r.t2 = 0;
     }
     const int tr = mu1 / g.T, tc = mu2 / g.T;
     const unsigned key = (static_cast<unsigned>(tr * g.tiles2 + tc) * g.T + (mu1 - tr * g.T)) * g.T + (mu2 - tc * g.T);
@@ -660,6 +676,7 @@ void destroy_plan(nfft2d_plan_s *p) {
     cudaFree(p->deap1);
     cudaFree(p->deap2);
     cudaFree(p->d_status);
+    cudaFreeHost(p->h_status);
     cudaFree(p->cell_count);
     cudaFree(p->scan_tmp);
     for (auto &e : p->timer.ev)
@@ -1072,6 +1089,8 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     if ((e = plan_malloc(reinterpret_cast<void **>(&p->deap1), rs * N1)) != cudaSuccess) return fail(status_from_cuda(e));
     if ((e = plan_malloc(reinterpret_cast<void **>(&p->deap2), rs * N2)) != cudaSuccess) return fail(status_from_cuda(e));
     if ((e = plan_malloc(reinterpret_cast<void **>(&p->d_status), 4 * sizeof(int))) != cudaSuccess) return fail(status_from_cuda(e));
+    if ((e = plan_malloc_host(reinterpret_cast<void **>(&p->h_status), 4 * sizeof(int))) != cudaSuccess)
+        return fail(status_from_cuda(e));
     if ((e = cudaMemsetAsync(p->d_status, 0, 4 * sizeof(int), p->stream)) != cudaSuccess)
         return fail(status_from_cuda(e));
 
@@ -1194,7 +1213,8 @@ int nfft2d_get_info(nfft2d_plan p, nfft2d_info *info) {
     return NFFT2D_OK;
 }
 
-static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
+static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units,
+                                  bool async) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
     if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
         return NFFT2D_ERR_INVALID_ARG;
@@ -1206,7 +1226,7 @@ static int nfft2d_set_points_impl(nfft2d_plan p, long long M, const void *x1, co
         u1 = p->N1 / (2.0 * kPi);
         u2 = p->N2 / (2.0 * kPi);
     }
-    return nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0);
+    return nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0, async);
 }
 
 // The address the binning kernel reads coordinates through: device or
@@ -1240,7 +1260,7 @@ static int coord_device_ptr(const nfft2d_plan_s *p, const void *x, const void **
 
 extern "C++" {
 int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype,
-                              double u1, double u2, double o1, double o2) {
+                              double u1, double u2, double o1, double o2, bool async) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
     if (M < 0 || M > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;
     if (coord_dtype != NFFT2D_COORD_F32 && coord_dtype != NFFT2D_COORD_F64) return NFFT2D_ERR_INVALID_ARG;
@@ -1319,8 +1339,16 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
                                       scan_state + scan_state_words(cells_n), p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
     stage_end(p, ST_SORT);
-    int hs[4] = {0, 0, 0, 0};
-    NFFT_TRY_CUDA(cudaMemcpyAsync(hs, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    if (async) {
+        // the work-item count stays on the device (status[0]); the kernels
+        // read it there, nfft2d_synchronize fetches it and reports errors
+        p->n_chunks = -1;
+        p->M = M;
+        p->points_valid = true;
+        return NFFT2D_OK;
+    }
+    const int *hs = p->h_status;  // page-locked: the read-back is one small DMA
+    NFFT_TRY_CUDA(cudaMemcpyAsync(p->h_status, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
     NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
     if (hs[1] & kErrNonfinite) return NFFT2D_ERR_NONFINITE;
     if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
@@ -1402,8 +1430,11 @@ static int nfft2d_type1_impl(nfft2d_plan p, int sign, const void *f, void *F) {
 static int nfft2d_grad_x_impl(nfft2d_plan p, int sign, const void *F, const void *v, void *g1, void *g2);
 
 int nfft2d_set_points(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
-    const int st = nfft2d_set_points_impl(p, M, x1, x2, coord_dtype, units);
-    return st;
+    return nfft2d_set_points_impl(p, M, x1, x2, coord_dtype, units, false);
+}
+
+int nfft2d_set_points_async(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
+    return nfft2d_set_points_impl(p, M, x1, x2, coord_dtype, units, true);
 }
 
 int nfft2d_type2(nfft2d_plan p, int sign, const void *F, void *f) {
@@ -1442,10 +1473,20 @@ static int nfft2d_grad_x_impl(nfft2d_plan p, int sign, const void *F, const void
 
 int nfft2d_synchronize(nfft2d_plan p) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
-    int hs[4] = {0, 0, 0, 0};
-    NFFT_TRY_CUDA(cudaMemcpyAsync(hs, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    const int *hs = p->h_status;
+    NFFT_TRY_CUDA(cudaMemcpyAsync(p->h_status, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
     NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
     NFFT_TRY_CUDA(cudaGetLastError());
+    if (p->points_valid && p->n_chunks < 0) {  // points set by nfft2d_set_points_async
+        if (hs[1] & kErrNonfinite) {
+            p->points_valid = false;
+            p->M = 0;
+            p->n_chunks = 0;
+            return NFFT2D_ERR_NONFINITE;
+        }
+        if (hs[0] < 0 || hs[0] > p->chunks_cap) return NFFT2D_ERR_INTERNAL;
+        p->n_chunks = hs[0];
+    }
     if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
     if (hs[1] & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
     return NFFT2D_OK;

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
     float2 *patch = bufs + warp * pstride;  // this warp's flush buffer, PR x 32
     constexpr int SP = point_scratch<K>();
     float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * SP;
-    const int n = a.n_chunks;
+    const int n = a.n_chunks >= 0 ? a.n_chunks : a.status[0];  // < 0: counted on the device only
     int *work = a.status + 2;  // work-item counter, zeroed before the launch
     bool pending = false;
 
@@ -138,9 +138,11 @@ cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
         cudaError_t e = cudaMemsetAsync(p->d_status + 2, 0, sizeof(int), p->stream);
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kSpreadWarps * 32, smem);
-        const long long items = p->n_chunks * ((p->chunk + kSpreadItem - 1) / kSpreadItem);
-        const int need = static_cast<int>((items + kSpreadWarps - 1) / kSpreadWarps);
-        if (blocks > need) blocks = need;
+        if (p->n_chunks >= 0) {  // else the count is on the device: the full persistent grid
+            const long long items = p->n_chunks * ((p->chunk + kSpreadItem - 1) / kSpreadItem);
+            const int need = static_cast<int>((items + kSpreadWarps - 1) / kSpreadWarps);
+            if (blocks > need) blocks = need;
+        }
         kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(p->tmap, static_cast<const Rec32 *>(p->recs),
                                                                 p->chunks, static_cast<const float2 *>(f), a);
         return cudaGetLastError();

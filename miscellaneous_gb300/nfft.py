@@ -123,9 +123,12 @@ class Plan:
         check(self._lib.nfft2d_synchronize(self._h), "nfft2d_synchronize")
 
     # -- points -------------------------------------------------------------
-    def set_points(self, x1: torch.Tensor, x2: torch.Tensor, units: str = "unit") -> None:
+    def set_points(self, x1: torch.Tensor, x2: torch.Tensor, units: str = "unit", sync: bool = True) -> None:
         """Bin and sort the points.  x1 pairs with N1 (rows), x2 with N2.
-        units: 'grid' (reference: period N), 'unit' (period 1) or 'radians'."""
+        units: 'grid' (reference: period N), 'unit' (period 1) or 'radians'.
+        sync=False returns once the binning is enqueued: the transforms that
+        follow on the plan's stream use the device-side result, and a
+        non-finite coordinate is reported by the next synchronize()."""
         if x1.shape != x2.shape or x1.dim() != 1:
             raise ValueError("x1 and x2 must be 1-D tensors of equal length")
         if x1.dtype not in (torch.float32, torch.float64) or x2.dtype != x1.dtype:
@@ -139,8 +142,8 @@ class Plan:
                 raise TypeError(f"{name} must be a CUDA tensor or a contiguous pinned CPU tensor")
         cd = _lib.COORD_F32 if x1.dtype == torch.float32 else _lib.COORD_F64
         M = x1.numel()
-        check(self._lib.nfft2d_set_points(self._h, M, _ptr(x1), _ptr(x2), cd, _lib.UNITS[units]),
-              "nfft2d_set_points")
+        fn = self._lib.nfft2d_set_points if sync else self._lib.nfft2d_set_points_async
+        check(fn(self._h, M, _ptr(x1), _ptr(x2), cd, _lib.UNITS[units]), "nfft2d_set_points")
         self.M = M
         self._keep = (x1, x2)
 

@@ -92,6 +92,8 @@ typedef struct {
     long long M;           /* points currently set (0 before set_points)        */
     long long n_chunks;    /* work items built by the last set_points           */
     size_t workspace_bytes;/* device bytes owned by the plan                    */
+    int fft_mode;          /* oversampled FFT in use: 0 2D cuFFT plan, 1 cuFFT
+                              passes, 2 fused passes (see nfft2d_tuning)       */
 } nfft2d_info;
 
 typedef struct {
@@ -100,11 +102,15 @@ typedef struct {
     int gather_variant;    /* NFFT2D_VARIANT_*                                  */
     int spread_variant;    /* NFFT2D_VARIANT_*                                  */
     int compensated;       /* -1 = default (on); 0 off; 1 on (FP32 gather)      */
-    int fft_pruned;        /* -1 = keep (initially: by grid size, two passes from
-                              2048 x 2048 oversampled cells up); 0: one 2D cuFFT
-                              plan; 1: two 1D passes, the column pass only over
-                              the columns the band needs (1.5 instead of 2
-                              passes at sigma = 2)                              */
+    int fft_mode;          /* -1 = keep.  Initially: 2 where it applies, else 1
+                              from 2048 x 2048 oversampled cells up, else 0.
+                              0: one 2D cuFFT plan; 1: two 1D cuFFT passes, the
+                              column pass only over the columns the band needs
+                              (1.5 instead of 2 passes at sigma = 2); 2: the
+                              library's own FFT passes fused with deapodize/pad,
+                              halo fill, halo fold and crop (FP32 plans, grid
+                              sides powers of two from 64 to 4096, else
+                              NFFT2D_ERR_UNSUPPORTED)                           */
 } nfft2d_tuning;
 
 /* Stage times in milliseconds, from CUDA events recorded on the plan's

@@ -45,6 +45,7 @@ class Info(ctypes.Structure):
         ("tiles2", ctypes.c_int), ("patch_rows", ctypes.c_int), ("patch_cols", ctypes.c_int),
         ("chunk", ctypes.c_int), ("gather_variant", ctypes.c_int), ("spread_variant", ctypes.c_int),
         ("M", ctypes.c_longlong), ("n_chunks", ctypes.c_longlong), ("workspace_bytes", ctypes.c_size_t),
+        ("fft_mode", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -53,7 +54,7 @@ class Info(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int), ("chunk", ctypes.c_int), ("gather_variant", ctypes.c_int),
-                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int), ("fft_pruned", ctypes.c_int)]
+                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int), ("fft_mode", ctypes.c_int)]
 
 
 class Timings(ctypes.Structure):

@@ -125,7 +125,9 @@ struct nfft2d_plan_s {
     bool fft_ok = false;
     cufftHandle fft_rows = 0, fft_cols = 0;  // pruned 1D passes (see run_fft)
     bool pruned_ok = false;
-    int fft_pruned = -1;                     // 1 use them, 0 don't, -1 by grid size
+    int fft_mode = -1;                       // -1 auto, 0 2D plan, 1 pruned passes, 2 fused passes
+    bool fused_ok = false;                   // twiddle tables of the fused passes are set up
+    float2 *tw1 = nullptr, *tw2 = nullptr;   // exp(-2 pi i m / n1), exp(-2 pi i m / n2)
     CUtensorMap tmap;  // 64-byte aligned by its own declaration
     bool tmap_ok = false;
 
@@ -183,6 +185,16 @@ int type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const void *c
 // allocation-failure hook used by the tests (NFFT2D_FAIL_ALLOC_AT).
 cudaError_t plan_malloc(void **ptr, size_t bytes);
 cudaError_t plan_malloc_host(void **ptr, size_t bytes);
+
+// The fused FFT passes (nfft2d_fft.cu): eligibility, per-plan twiddle tables,
+// type 2 = deapodize/pad + band-column FFT, then row FFT + halo fill;
+// type 1 = halo fold + row FFT, then band-column FFT + crop/deapodize.
+bool fused_fft_eligible(int precision, int n1, int n2);
+int setup_fused_fft(nfft2d_plan_s *p);
+cudaError_t fused_type2_cols(const nfft2d_plan_s *p, int sign, const void *F);
+cudaError_t fused_type2_rows(const nfft2d_plan_s *p, int sign);
+cudaError_t fused_type1_rows(const nfft2d_plan_s *p, int sign);
+cudaError_t fused_type1_cols(const nfft2d_plan_s *p, int sign, void *F);
 
 // Host FP64 helpers shared by the plan and the Knab regridder.
 double bessel_i0_host(double x);

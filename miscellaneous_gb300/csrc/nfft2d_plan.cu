@@ -148,6 +148,16 @@ namespace {
 
 constexpr double kPi = 3.141592653589793238462643383279502884;
 
+// The fused FFT passes (nfft2d_fft.cu) serve FP32 plans on power-of-two
+// grids unless a cuFFT mode was chosen.
+bool use_fused(const nfft2d_plan_s *p) { return p->fused_ok && (p->fft_mode == 2 || p->fft_mode < 0); }
+
+int fft_mode_in_use(const nfft2d_plan_s *p) {
+    if (use_fused(p)) return 2;
+    const bool pruned = p->fft_mode == 1 || (p->fft_mode < 0 && 1LL * p->g.n1 * p->g.n2 >= 2048LL * 2048LL);
+    return pruned && p->pruned_ok ? 1 : 0;
+}
+
 // ---------------------------------------------------------------------------
 // host math (plan time, FP64)
 // ---------------------------------------------------------------------------
@@ -677,6 +687,8 @@ void destroy_plan(nfft2d_plan_s *p) {
     cudaFree(p->deap2);
     cudaFree(p->d_status);
     cudaFreeHost(p->h_status);
+    cudaFree(p->tw1);
+    cudaFree(p->tw2);
     cudaFree(p->cell_count);
     cudaFree(p->scan_tmp);
     for (auto &e : p->timer.ev)
@@ -761,6 +773,10 @@ int setup_grid(nfft2d_plan_s *p) {
                 cufftDestroy(p->fft_rows);
             }
         }
+    }
+    if (!p->grid_external) {
+        const int st = setup_fused_fft(p);
+        if (st != NFFT2D_OK) return st;
     }
     if (p->precision == NFFT2D_F32) return make_tensor_map(p);
     return NFFT2D_OK;
@@ -943,7 +959,7 @@ int run_fft(nfft2d_plan_s *p, int sign, bool type2) {
     // by default the two passes run from 2048 x 2048 oversampled cells up:
     // below that cuFFT's single 2D plan is faster on GB300 (1024^2: 20 us
     // vs 30 us; 2048^2: 40 vs 35 us; 4096^2: 153 vs 112 us)
-    const bool pruned = p->fft_pruned > 0 || (p->fft_pruned < 0 && 1LL * g.n1 * g.n2 >= 2048LL * 2048LL);
+    const bool pruned = p->fft_mode == 1 || (p->fft_mode < 0 && 1LL * g.n1 * g.n2 >= 2048LL * 2048LL);
     if (!(pruned && p->pruned_ok)) return status_from_cufft(exec_at(p, p->fft, off, dir));
     const size_t right = off + static_cast<size_t>(g.n2 - p->N2 / 2);  // first column of the negative band
     cufftResult r;
@@ -957,7 +973,17 @@ int run_fft(nfft2d_plan_s *p, int sign, bool type2) {
     return status_from_cufft(exec_at(p, p->fft_cols, right, dir));
 }
 
+
 int type2_prepare(nfft2d_plan_s *p, int sign, const void *F) {
+    if (use_fused(p)) {  // pad + band-column FFT, then row FFT + halo fill
+        stage_begin(p, ST_PAD);
+        NFFT_TRY_CUDA(fused_type2_cols(p, sign, F));
+        stage_end(p, ST_PAD);
+        stage_begin(p, ST_FFT2);
+        NFFT_TRY_CUDA(fused_type2_rows(p, sign));
+        stage_end(p, ST_FFT2);
+        return NFFT2D_OK;
+    }
     stage_begin(p, ST_PAD);
     NFFT_TRY_CUDA(launch_pad(p, F));
     stage_end(p, ST_PAD);
@@ -1181,7 +1207,9 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     p->gather_variant = gv;
     p->spread_variant = sv;
     if (t->compensated >= 0) p->compensated = t->compensated ? 1 : 0;
-    if (t->fft_pruned >= 0) p->fft_pruned = t->fft_pruned ? 1 : 0;
+    if (t->fft_mode > 2 || t->fft_mode < -1) return NFFT2D_ERR_INVALID_ARG;
+    if (t->fft_mode == 2 && !p->fused_ok) return NFFT2D_ERR_UNSUPPORTED;
+    if (t->fft_mode >= 0) p->fft_mode = t->fft_mode;
     p->workspace_bytes = plan_workspace_bytes(p);
     return NFFT2D_OK;
 }
@@ -1210,6 +1238,7 @@ int nfft2d_get_info(nfft2d_plan p, nfft2d_info *info) {
     info->M = p->points_valid ? p->M : 0;
     info->n_chunks = p->points_valid ? p->n_chunks : 0;
     info->workspace_bytes = p->workspace_bytes;
+    info->fft_mode = fft_mode_in_use(p);
     return NFFT2D_OK;
 }
 
@@ -1414,6 +1443,15 @@ static int nfft2d_type1_impl(nfft2d_plan p, int sign, const void *f, void *F) {
     NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C, p->stream));
     NFFT_TRY_CUDA(launch_spread(p, f));
     stage_end(p, ST_SPREAD);
+    if (use_fused(p)) {  // fold + row FFT, then band-column FFT + crop
+        stage_begin(p, ST_FOLD);
+        NFFT_TRY_CUDA(fused_type1_rows(p, sign));
+        stage_end(p, ST_FOLD);
+        stage_begin(p, ST_FFT1);
+        NFFT_TRY_CUDA(fused_type1_cols(p, sign, F));
+        stage_end(p, ST_FFT1);
+        return NFFT2D_OK;
+    }
     stage_begin(p, ST_FOLD);
     NFFT_TRY_CUDA(launch_halo_fold(p));
     stage_end(p, ST_FOLD);

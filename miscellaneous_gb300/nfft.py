@@ -102,8 +102,11 @@ class Plan:
         check(self._lib.nfft2d_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "nfft2d_set_stream")
 
     def set_tuning(self, tile: int = 0, chunk: int = 0, gather_variant: int = 0, spread_variant: int = 0,
-                   compensated: int = -1, fft_pruned: int = -1) -> None:
-        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated, fft_pruned)
+                   compensated: int = -1, fft_mode: int = -1) -> None:
+        """fft_mode: -1 keep, 0 cuFFT 2D plan, 1 cuFFT row/band-column passes,
+        2 hand-written passes fused with pad/fill/fold/crop (FP32, power-of-two
+        grids; the default where it applies)."""
+        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated, fft_mode)
         check(self._lib.nfft2d_set_tuning(self._h, ctypes.byref(t)), "nfft2d_set_tuning")
 
     def info(self) -> dict:

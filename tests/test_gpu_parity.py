@@ -250,7 +250,36 @@ def test_pruned_fft_matches_full_fft(N1, N2, sigma, prec, tol):
     to ~92x by the deapodization at sigma = 1.25, as against the oracle)."""
     F, x1, x2, f = _inputs(N1, N2, 3000, seed=21)
     kw = {"sigma": sigma, "K": 6, "precision": prec}
-    a = _run(kw, F, x1, x2, f, tuning={"fft_pruned": 1})
-    b = _run(kw, F, x1, x2, f, tuning={"fft_pruned": 0})
+    a = _run(kw, F, x1, x2, f, tuning={"fft_mode": 1})
+    b = _run(kw, F, x1, x2, f, tuning={"fft_mode": 0})
     for u, v in zip(a[:3], b[:3]):
         assert np.linalg.norm(u - v) / np.linalg.norm(v) < tol
+
+
+@pytest.mark.parametrize("N1,N2,K", [(32, 32, 6), (64, 32, 4), (32, 512, 6), (512, 512, 6), (256, 1024, 8),
+                                     (2048, 64, 3), (128, 2048, 6)])
+def test_fused_fft_matches_cufft(N1, N2, K):
+    """The library's own FFT passes fused with pad / halo fill / halo fold /
+    crop (fft_mode 2, the default on power-of-two grids) give the same
+    forward, adjoint and reference-sign spread as cuFFT's 2D plan around the
+    separate stage kernels, to FP32 rounding (FFT sizes 64 .. 4096, square,
+    tall and wide grids)."""
+    F, x1, x2, f = _inputs(N1, N2, 5000, seed=N1 + N2)
+    kw = {"sigma": 2.0, "K": K}
+    a = _run(kw, F, x1, x2, f, tuning={"fft_mode": 2})
+    b = _run(kw, F, x1, x2, f, tuning={"fft_mode": 0})
+    for u, v in zip(a[:3], b[:3]):
+        assert np.linalg.norm(u - v) / np.linalg.norm(v) < 2e-6
+
+
+def test_fused_fft_mode_unsupported_off_power_of_two():
+    from miscellaneous_gb300 import _lib
+    from miscellaneous_gb300.nfft import Plan
+    with Plan(48, 24, sigma=1.25) as p:  # 60 x 30 oversampled cells
+        with pytest.raises(_lib.NFFT2DError) as e:
+            p.set_tuning(fft_mode=2)
+        assert e.value.status == _lib.ERR_UNSUPPORTED
+    with Plan(64, 64, precision="f64") as p:
+        with pytest.raises(_lib.NFFT2DError) as e:
+            p.set_tuning(fft_mode=2)
+        assert e.value.status == _lib.ERR_UNSUPPORTED

@@ -44,6 +44,9 @@ namespace {
 
 constexpr int kFftMaxElems = 4096;  // complex elements per CTA (P * n): 256 threads
 constexpr int kFftMinElems = 1024;  // at least 64 threads per CTA
+// The kernels declare two CTAs of the largest shape per SM (at most 128
+// registers a thread): the fold pass otherwise took 145 and its 512 CTAs of
+// 128 threads no longer fitted in one wave on GB300 (14 vs 18 us).
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -115,11 +118,6 @@ __device__ __forceinline__ void dft8(float2 *y, float s) {
     }
 }
 
-// In-place Stockham FFT of P sequences of length N = 2^logN in (padded)
-// shared memory, X_k = sum_m x_m exp(s 2 pi i m k / N).  blockDim.x must be
-// P N / 16: every thread holds 16 elements per stage -- one radix-16
-// butterfly, or 16/R butterflies of the first stage (radix R = 2^(logN mod
-// 4), no twiddles), loaded before a barrier and stored after it.
 // First stage of a length whose log2 is not a multiple of 4: radix R (2, 4
 // or 8) at L = 1 (no twiddles), 16/R butterflies per thread.
 template <int R, bool INTERLEAVED>
@@ -162,13 +160,40 @@ __device__ __forceinline__ void first_stage(float2 *buf, int logN, int logP, flo
     __syncthreads();
 }
 
+// The table twiddles of a thread's radix-16 butterflies (at most three
+// radix-16 stages for N <= 4096): exp(s 2 pi i j r / 16L) for r = 1, 2, 4, 8.
+// Loaded at kernel start so their latency hides behind the grid loads.
+struct Twiddles {
+    float2 w[3][4];
+};
+
+template <bool INTERLEAVED>
+__device__ __forceinline__ void prefetch_twiddles(Twiddles &T, int logN, int logP, float s,
+                                                  const float2 *__restrict__ tw) {
+    const int t = threadIdx.x, logQ = logN - 4;
+    const int b = INTERLEAVED ? (t >> logP) : (t & ((1 << logQ) - 1));
+#pragma unroll
+    for (int st = 0; st < 3; ++st) {
+        const int logL = (logN & 3) + 4 * st;
+        if (logL >= logN) break;
+        const int j = b & ((1 << logL) - 1);
+        const int m = j << (logN - logL - 4);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            float2 w = __ldg(tw + (m << e));
+            if (s > 0) w.y = -w.y;  // the table holds exp(-2 pi i m / N)
+            T.w[st][e] = w;
+        }
+    }
+}
+
 // In-place Stockham FFT of P sequences of length N = 2^logN in (padded)
 // shared memory, X_k = sum_m x_m exp(s 2 pi i m k / N).  blockDim.x must be
 // P N / 16: every thread holds 16 elements per stage -- one radix-16
 // butterfly, or 16/R butterflies of the first stage (radix R = 2^(logN mod
 // 4), no twiddles), loaded before a barrier and stored after it.
 template <bool INTERLEAVED>
-__device__ void fft_inplace(float2 *buf, int logN, int logP, float s, const float2 *__restrict__ tw) {
+__device__ void fft_inplace(float2 *buf, int logN, int logP, float s, const Twiddles &tws) {
     const int t = threadIdx.x;
     const int rem = logN & 3;
     if (rem == 1) first_stage<2, INTERLEAVED>(buf, logN, logP, s);
@@ -177,7 +202,9 @@ __device__ void fft_inplace(float2 *buf, int logN, int logP, float s, const floa
     int logL = rem;
     float2 y[16];
     const int logQ = logN - 4;  // N/16 butterflies per sequence
-    for (; logL < logN; logL += 4) {
+#pragma unroll
+    for (int st = 0; st < 3; ++st, logL += 4) {
+        if (logL >= logN) break;
         const int L = 1 << logL;
         const int q = INTERLEAVED ? (t & ((1 << logP) - 1)) : (t >> logQ);
         const int b = INTERLEAVED ? (t >> logP) : (t & ((1 << logQ) - 1));
@@ -186,21 +213,13 @@ __device__ void fft_inplace(float2 *buf, int logN, int logP, float s, const floa
         for (int r = 0; r < 16; ++r) y[r] = buf[at<INTERLEAVED>(q, b + (r << logQ), logP, logN)];
         __syncthreads();
         if (j) {
-            // w^r = exp(s 2 pi i j r / 16L): powers 1, 2, 4, 8 from the table
-            // (which holds exp(-2 pi i m / N)), the rest as products of at
-            // most three of them
-            const int m = j << (logN - logL - 4);
+            // w^r = exp(s 2 pi i j r / 16L): powers 1, 2, 4, 8 from the table,
+            // the rest as products of at most three of them
             float2 w[16];
-            w[1] = __ldg(tw + m);
-            w[2] = __ldg(tw + 2 * m);
-            w[4] = __ldg(tw + 4 * m);
-            w[8] = __ldg(tw + 8 * m);
-            if (s > 0) {
-                w[1].y = -w[1].y;
-                w[2].y = -w[2].y;
-                w[4].y = -w[4].y;
-                w[8].y = -w[8].y;
-            }
+            w[1] = tws.w[st][0];
+            w[2] = tws.w[st][1];
+            w[4] = tws.w[st][2];
+            w[8] = tws.w[st][3];
             w[3] = cmul(w[1], w[2]);
             w[5] = cmul(w[4], w[1]);
             w[6] = cmul(w[4], w[2]);
@@ -234,11 +253,13 @@ struct FftArgs {
 };
 
 // Type 2, pass 1: P band columns per CTA.
-__global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_cols_pad(const float2 *__restrict__ F, float2 *__restrict__ grid,
+__global__ void __launch_bounds__(kFftMaxElems / 16, 2) k_fft_cols_pad(const float2 *__restrict__ F, float2 *__restrict__ grid,
                                                               const float *__restrict__ d1,
                                                               const float *__restrict__ d2,
                                                               const float2 *__restrict__ tw, const FftArgs a) {
     extern __shared__ float2 fsm[];
+    Twiddles tws;
+    prefetch_twiddles<true>(tws, a.logn1, a.logP, a.s, tw);
     const int P = 1 << a.logP, n1 = a.n1;
     const int bc0 = blockIdx.x << a.logP;
     // every thread owns 16 elements (blockDim = P n / 16): all loads first
@@ -259,7 +280,7 @@ __global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_cols_pad(const float2
 #pragma unroll
     for (int u = 0; u < 16; ++u) fsm[pad16(threadIdx.x + u * blockDim.x)] = v[u];
     __syncthreads();
-    fft_inplace<true>(fsm, a.logn1, a.logP, a.s, tw);
+    fft_inplace<true>(fsm, a.logn1, a.logP, a.s, tws);
     const int q = threadIdx.x & (P - 1), bc = bc0 + q;  // blockDim is a multiple of P
     if (bc >= a.N2) return;
     float2 *col = grid + static_cast<size_t>(a.H) * a.C + a.H + band_col(bc, a.N2, a.n2);
@@ -272,9 +293,11 @@ __global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_cols_pad(const float2
 // the column-transformed grid is zero), the whole row and its halo images
 // are written: side halo columns for every row, and for the first and last
 // H rows the full padded row (every allocated column) in the halo rows.
-__global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_rows_fill(float2 *__restrict__ grid,
+__global__ void __launch_bounds__(kFftMaxElems / 16, 2) k_fft_rows_fill(float2 *__restrict__ grid,
                                                                const float2 *__restrict__ tw, const FftArgs a) {
     extern __shared__ float2 fsm[];
+    Twiddles tws;
+    prefetch_twiddles<false>(tws, a.logn2, a.logP, a.s, tw);
     const int n2 = a.n2;
     const int r0 = blockIdx.x << a.logP;
     {
@@ -291,7 +314,7 @@ __global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_rows_fill(float2 *__r
         for (int u = 0; u < 16; ++u) fsm[pad16(threadIdx.x + u * blockDim.x)] = v[u];
     }
     __syncthreads();
-    fft_inplace<false>(fsm, a.logn2, a.logP, a.s, tw);
+    fft_inplace<false>(fsm, a.logn2, a.logP, a.s, tws);
     const int P = 1 << a.logP;
     for (int q = 0; q < P; ++q) {
         const int r = r0 + q;
@@ -321,35 +344,47 @@ __global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_rows_fill(float2 *__r
 // images inside the logical padded grid (R x Cl), the row is transformed and
 // only its band columns are written back (in place: a CTA reads other rows'
 // images only in halo rows and columns, which no CTA writes).
-__global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_rows_fold(float2 *__restrict__ grid,
+__global__ void __launch_bounds__(kFftMaxElems / 16, 2) k_fft_rows_fold(float2 *__restrict__ grid,
                                                                const float2 *__restrict__ tw, const FftArgs a) {
     extern __shared__ float2 fsm[];
+    Twiddles tws;
     const int n2 = a.n2, n1 = a.n1;
     const int r0 = blockIdx.x << a.logP;
+    // images inside the logical padded grid R x Cl = (n1 + 2H) x (n2 + 2H):
+    // columns c < H and c >= n2 - H have one side image, rows r < H and
+    // r >= n1 - H one row image (with its side image at the corners); only
+    // CTAs holding edge rows look at row images
     float2 vs[16];
+    const int H = a.H;
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
         const int e = threadIdx.x + u * blockDim.x;
         const int q = e >> a.logn2, c = e & (n2 - 1);
-        const int pr0 = r0 + q + a.H, pc0 = c + a.H;
-        float2 v = grid[static_cast<size_t>(pr0) * a.C + pc0];
-        const bool up = pr0 - n1 >= 0, down = pr0 + n1 < a.R;
-        const bool left = pc0 - n2 >= 0, right = pc0 + n2 < a.Cl;
-        if (up || down || left || right) {
-            for (int da = -1; da <= 1; ++da) {
-                if ((da < 0 && !up) || (da > 0 && !down)) continue;
-                for (int db = -1; db <= 1; ++db) {
-                    if ((da == 0 && db == 0) || (db < 0 && !left) || (db > 0 && !right)) continue;
-                    v = cadd(v, grid[static_cast<size_t>(pr0 + da * n1) * a.C + pc0 + db * n2]);
-                }
-            }
-        }
+        const float2 *src = grid + static_cast<size_t>(r0 + q + H) * a.C + H + c;
+        float2 v = *src;
+        const int dc = c < H ? n2 : (c >= n2 - H ? -n2 : 0);
+        if (dc) v = cadd(v, src[dc]);
         vs[u] = v;
+    }
+    if (r0 < H || r0 + (1 << a.logP) > n1 - H) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int e = threadIdx.x + u * blockDim.x;
+            const int r = r0 + (e >> a.logn2), c = e & (n2 - 1);
+            const int dr = r < H ? n1 : (r >= n1 - H ? -n1 : 0);
+            if (!dr) continue;
+            const float2 *src = grid + static_cast<size_t>(r + H + dr) * a.C + H + c;
+            float2 v = cadd(vs[u], *src);
+            const int dc = c < H ? n2 : (c >= n2 - H ? -n2 : 0);
+            if (dc) v = cadd(v, src[dc]);
+            vs[u] = v;
+        }
     }
 #pragma unroll
     for (int u = 0; u < 16; ++u) fsm[pad16(threadIdx.x + u * blockDim.x)] = vs[u];
+    prefetch_twiddles<false>(tws, a.logn2, a.logP, a.s, tw);
     __syncthreads();
-    fft_inplace<false>(fsm, a.logn2, a.logP, a.s, tw);
+    fft_inplace<false>(fsm, a.logn2, a.logP, a.s, tws);
     for (int e = threadIdx.x; e < (a.N2 << a.logP); e += blockDim.x) {
         const int q = e / a.N2, bc = e - q * a.N2;
         const int c = band_col(bc, a.N2, n2);
@@ -359,11 +394,13 @@ __global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_rows_fold(float2 *__r
 
 // Type 1, pass 2: P band columns per CTA, transformed, cropped to the N1 band
 // rows and deapodized into F (N1 x N2, row-major).
-__global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_cols_crop(const float2 *__restrict__ grid, float2 *__restrict__ F,
+__global__ void __launch_bounds__(kFftMaxElems / 16, 2) k_fft_cols_crop(const float2 *__restrict__ grid, float2 *__restrict__ F,
                                                                const float *__restrict__ d1,
                                                                const float *__restrict__ d2,
                                                                const float2 *__restrict__ tw, const FftArgs a) {
     extern __shared__ float2 fsm[];
+    Twiddles tws;
+    prefetch_twiddles<true>(tws, a.logn1, a.logP, a.s, tw);
     const int P = 1 << a.logP, n1 = a.n1;
     const int bc0 = blockIdx.x << a.logP;
     {
@@ -379,7 +416,7 @@ __global__ void __launch_bounds__(kFftMaxElems / 16) k_fft_cols_crop(const float
         for (int u = 0; u < 16; ++u) fsm[pad16(threadIdx.x + u * blockDim.x)] = v[u];
     }
     __syncthreads();
-    fft_inplace<true>(fsm, a.logn1, a.logP, a.s, tw);
+    fft_inplace<true>(fsm, a.logn1, a.logP, a.s, tws);
     // blockDim is a multiple of P, so a thread keeps one column q
     const int q = threadIdx.x & (P - 1), bc = bc0 + q;
     if (bc >= a.N2) return;
@@ -402,11 +439,14 @@ int ilog2(int n) {
 }
 
 // sequences per CTA: up to kFftMaxElems elements, fewer while that leaves
-// under two CTAs per SM, but not under kFftMinElems (or one sequence)
-int seqs_log(int logn, int seqs, int num_sms) {
+// under min_ctas CTAs, but not under kFftMinElems (or one sequence).  The
+// thread count (16 elements each) does not depend on it: the column passes
+// keep more columns per CTA (one 32-byte sector per row at P = 4) and accept
+// fewer, larger CTAs.
+int seqs_log(int logn, int seqs, int min_ctas) {
     int logP = ilog2(kFftMaxElems) - logn;
     if (logP < 0) logP = 0;
-    while (logP > 0 && (seqs >> logP) < 2 * num_sms && (1 << (logn + logP - 1)) >= kFftMinElems) --logP;
+    while (logP > 0 && (seqs >> logP) < min_ctas && (1 << (logn + logP - 1)) >= kFftMinElems) --logP;
     return logP;
 }
 
@@ -467,7 +507,7 @@ int setup_fused_fft(nfft2d_plan_s *p) {
 
 cudaError_t fused_type2_cols(const nfft2d_plan_s *p, int sign, const void *F) {
     FftArgs a = fft_args(p, sign);
-    a.logP = seqs_log(a.logn1, p->N2, p->num_sms);
+    a.logP = seqs_log(a.logn1, p->N2, p->num_sms / 2);
     const int blocks = (p->N2 + (1 << a.logP) - 1) >> a.logP;
     const int threads = (a.n1 << a.logP) / 16;
     const int smem = padded_elems(a.n1 << a.logP) * static_cast<int>(sizeof(float2));
@@ -481,7 +521,7 @@ cudaError_t fused_type2_cols(const nfft2d_plan_s *p, int sign, const void *F) {
 
 cudaError_t fused_type2_rows(const nfft2d_plan_s *p, int sign) {
     FftArgs a = fft_args(p, sign);
-    a.logP = seqs_log(a.logn2, a.n1, p->num_sms);
+    a.logP = seqs_log(a.logn2, a.n1, 2 * p->num_sms);
     const int blocks = a.n1 >> a.logP;
     const int threads = (a.n2 << a.logP) / 16;
     const int smem = padded_elems(a.n2 << a.logP) * static_cast<int>(sizeof(float2));
@@ -493,7 +533,7 @@ cudaError_t fused_type2_rows(const nfft2d_plan_s *p, int sign) {
 
 cudaError_t fused_type1_rows(const nfft2d_plan_s *p, int sign) {
     FftArgs a = fft_args(p, sign);
-    a.logP = seqs_log(a.logn2, a.n1, p->num_sms);
+    a.logP = seqs_log(a.logn2, a.n1, 2 * p->num_sms);
     const int blocks = a.n1 >> a.logP;
     const int threads = (a.n2 << a.logP) / 16;
     const int smem = padded_elems(a.n2 << a.logP) * static_cast<int>(sizeof(float2));
@@ -505,7 +545,7 @@ cudaError_t fused_type1_rows(const nfft2d_plan_s *p, int sign) {
 
 cudaError_t fused_type1_cols(const nfft2d_plan_s *p, int sign, void *F) {
     FftArgs a = fft_args(p, sign);
-    a.logP = seqs_log(a.logn1, p->N2, p->num_sms);
+    a.logP = seqs_log(a.logn1, p->N2, p->num_sms / 2);
     const int blocks = (p->N2 + (1 << a.logP) - 1) >> a.logP;
     const int threads = (a.n1 << a.logP) / 16;
     const int smem = padded_elems(a.n1 << a.logP) * static_cast<int>(sizeof(float2));

@@ -948,7 +948,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fft-mode", choices=["auto", "cufft", "pruned", "fused"], default="auto",
-                    help="oversampled FFT: auto (fused passes where they apply), cuFFT 2D plan, cuFFT passes, fused")
+                    help="oversampled FFT: auto (fused passes below 2048^2 cells, else cuFFT), cuFFT 2D plan, "
+                         "cuFFT passes, fused")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
     ap.add_argument("--K", type=int, default=None, help="window half-width for the clustered workload (4, 6, 8)")

@@ -102,8 +102,9 @@ typedef struct {
     int gather_variant;    /* NFFT2D_VARIANT_*                                  */
     int spread_variant;    /* NFFT2D_VARIANT_*                                  */
     int compensated;       /* -1 = default (on); 0 off; 1 on (FP32 gather)      */
-    int fft_mode;          /* -1 = keep.  Initially: 2 where it applies, else 1
-                              from 2048 x 2048 oversampled cells up, else 0.
+    int fft_mode;          /* -1 = keep.  Initially automatic: 2 below 2048 x
+                              2048 oversampled cells where it applies, else 1
+                              from 2048 x 2048 cells up, else 0.
                               0: one 2D cuFFT plan; 1: two 1D cuFFT passes, the
                               column pass only over the columns the band needs
                               (1.5 instead of 2 passes at sigma = 2); 2: the

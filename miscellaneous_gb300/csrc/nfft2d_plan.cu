@@ -149,8 +149,16 @@ namespace {
 constexpr double kPi = 3.141592653589793238462643383279502884;
 
 // The fused FFT passes (nfft2d_fft.cu) serve FP32 plans on power-of-two
-// grids unless a cuFFT mode was chosen.
-bool use_fused(const nfft2d_plan_s *p) { return p->fused_ok && (p->fft_mode == 2 || p->fft_mode < 0); }
+// grids: by default below 2048 x 2048 oversampled cells, where they beat
+// cuFFT with the separate pad / fill / fold / crop kernels on GB300 (both
+// directions at 1024^2: 51 vs 71 us; 2048^2: 110 vs 108 us for the pruned
+// cuFFT passes; 4096^2: 421 vs 292 us, the column passes then holding one
+// column per CTA), or whenever fft_mode 2 asks for them.
+bool use_fused(const nfft2d_plan_s *p) {
+    if (!p->fused_ok) return false;
+    if (p->fft_mode == 2) return true;
+    return p->fft_mode < 0 && 1LL * p->g.n1 * p->g.n2 < 2048LL * 2048LL;
+}
 
 int fft_mode_in_use(const nfft2d_plan_s *p) {
     if (use_fused(p)) return 2;

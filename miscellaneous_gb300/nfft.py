@@ -105,7 +105,7 @@ class Plan:
                    compensated: int = -1, fft_mode: int = -1) -> None:
         """fft_mode: -1 keep, 0 cuFFT 2D plan, 1 cuFFT row/band-column passes,
         2 hand-written passes fused with pad/fill/fold/crop (FP32, power-of-two
-        grids; the default where it applies)."""
+        grids; the default below 2048 x 2048 oversampled cells)."""
         t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated, fft_mode)
         check(self._lib.nfft2d_set_tuning(self._h, ctypes.byref(t)), "nfft2d_set_tuning")
 

@@ -507,63 +507,75 @@ __global__ void k_bin_scatter(const RecT *__restrict__ tmp, const unsigned *__re
 // ---------------------------------------------------------------------------
 // single-pass exclusive scans (decoupled look-back)
 // ---------------------------------------------------------------------------
-// Blocks take tiles of kScanTile consecutive counters in launch order from a
-// ticket counter, scan them locally, publish the tile's aggregate, then walk
-// back over the predecessors' published words until one carries its
-// inclusive prefix.  A tile only waits on tiles whose blocks took earlier
-// tickets (already running), and every wait is bounded: a block that gives up
-// latches kErrTimeout and treats the missing value as 0, so the host sees an
-// error status instead of a hang.  One launch replaces the three-phase
-// reduce / scan-of-sums / apply sequence.
-constexpr int kScanThreads = 512;
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kScanThreads * kScanItems;
+// Blocks take tiles of consecutive counters in launch order from a ticket
+// counter, scan them locally, publish the tile's aggregate, then look back
+// over the predecessors' published words -- 32 at a time, one per lane of
+// the first warp -- until one carries its inclusive prefix.  A tile only
+// waits on tiles whose blocks took earlier tickets (already running), and
+// every wait is bounded: a lane that gives up latches kErrTimeout and counts
+// the missing value as 0, so the host sees an error status instead of a
+// hang.  One launch replaces the three-phase reduce / scan-of-sums / apply
+// sequence.
+constexpr int kCellScanThreads = 512, kCellScanItems = 8;  // 4096 cell counters per tile
+constexpr int kItemScanThreads = 128, kItemScanItems = 1;  // 128 bin tiles per tile
 constexpr unsigned long long kTileAggregate = 1ull << 32;
 constexpr unsigned long long kTilePrefix = 2ull << 32;
 
-// Scan state for one scan over n counters: a ticket counter (as a 64-bit
-// word) followed by one status word per tile.
-size_t scan_state_words(size_t n) { return 1 + (n + kScanTile - 1) / kScanTile; }
+// Scan state for one scan over n counters in tiles of `tile_elems`: a ticket
+// counter (as a 64-bit word) followed by one status word per tile.
+size_t scan_state_words(size_t n, int tile_elems) { return 1 + (n + tile_elems - 1) / tile_elems; }
 
-// The block's exclusive offset of this tile among all tiles; `agg` is the
-// tile's own sum.  Called by thread 0 only.
+// The exclusive offset of this tile among all tiles; `agg` is the tile's own
+// sum.  Called by all lanes of warp 0; the result is valid in every lane.
 __device__ unsigned tile_lookback(unsigned long long *tile_word, int tile, unsigned agg, int *status) {
+    const int lane = threadIdx.x & 31;
     if (tile == 0) {
-        atomicExch(tile_word, kTilePrefix | agg);
+        if (lane == 0) atomicExch(tile_word, kTilePrefix | agg);
         return 0u;
     }
-    atomicExch(tile_word + tile, kTileAggregate | agg);
+    if (lane == 0) atomicExch(tile_word + tile, kTileAggregate | agg);
     unsigned excl = 0;
-    for (int j = tile - 1; j >= 0; --j) {
-        unsigned long long w = 0;
-        uint32_t spins = 0;
-        for (;;) {
-            w = *reinterpret_cast<volatile unsigned long long *>(tile_word + j);
-            if (w >> 32) break;
-            if (++spins >= kSpinLimit) break;
-            if (spins > 16) __nanosleep(64);
+    for (int base = tile - 1;; base -= 32) {
+        const int j = base - lane;  // lane 0: the nearest predecessor
+        unsigned long long w = kTilePrefix;  // before tile 0: an inclusive prefix of 0
+        if (j >= 0) {
+            uint32_t spins = 0;
+            for (;;) {
+                w = *reinterpret_cast<volatile unsigned long long *>(tile_word + j);
+                if (w >> 32) break;
+                if (++spins >= kSpinLimit) break;
+                if (spins > 16) __nanosleep(64);
+            }
+            if (!(w >> 32)) {
+                latch_error(status, kErrTimeout);
+                w = kTilePrefix;  // give up here: count it as a prefix of 0
+            }
         }
-        if (!(w >> 32)) {
-            latch_error(status, kErrTimeout);
-            break;
-        }
-        excl += static_cast<unsigned>(w);
-        if ((w >> 32) == (kTilePrefix >> 32)) break;
+        const unsigned prefix_lanes = __ballot_sync(0xffffffffu, (w >> 32) == (kTilePrefix >> 32));
+        // the nearest prefix ends the walk: add lanes 0 .. k (k = its lane)
+        const int k = prefix_lanes ? __ffs(prefix_lanes) - 1 : 31;
+        unsigned v = lane <= k ? static_cast<unsigned>(w) : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        excl += v;
+        if (prefix_lanes) break;
     }
-    atomicExch(tile_word + tile, kTilePrefix | (excl + agg));
+    if (lane == 0) atomicExch(tile_word + tile, kTilePrefix | (excl + agg));
     return excl;
 }
 
-// Exclusive scan of the block's kScanTile items (v: the thread's
-// kScanItems consecutive values) across all tiles: returns the exclusive
-// prefix of the thread's first item.  `state` is the scan's ticket + words.
-__device__ unsigned block_scan_lookback(const unsigned (&v)[kScanItems], int tile, unsigned long long *state,
+// Exclusive scan of the block's THREADS * ITEMS items (v: the thread's ITEMS
+// consecutive values) across all tiles: returns the exclusive prefix of the
+// thread's first item.  `state` is the scan's ticket + words.
+template <int THREADS, int ITEMS>
+__device__ unsigned block_scan_lookback(const unsigned (&v)[ITEMS], int tile, unsigned long long *state,
                                         int *status) {
-    __shared__ unsigned warp_tot[kScanThreads / 32];
+    constexpr int WARPS = THREADS / 32;
+    __shared__ unsigned warp_tot[WARPS];
     __shared__ unsigned block_agg, block_excl;
     unsigned tsum = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) tsum += v[k];
+    for (int k = 0; k < ITEMS; ++k) tsum += v[k];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned incl = tsum;
 #pragma unroll
@@ -574,18 +586,21 @@ __device__ unsigned block_scan_lookback(const unsigned (&v)[kScanItems], int til
     if (lane == 31) warp_tot[wid] = incl;
     __syncthreads();
     if (wid == 0) {
-        const unsigned w = lane < kScanThreads / 32 ? warp_tot[lane] : 0u;
+        const unsigned w = lane < WARPS ? warp_tot[lane] : 0u;
         unsigned wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
             if (lane >= o) wi += y;
         }
-        if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
-        if (lane == 31) block_agg = wi;
+        if (lane < WARPS) warp_tot[lane] = wi - w;
+        const unsigned agg = __shfl_sync(0xffffffffu, wi, 31);
+        const unsigned ex = tile_lookback(state + 1, tile, agg, status);
+        if (lane == 0) {
+            block_agg = agg;
+            block_excl = ex;
+        }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) block_excl = tile_lookback(state + 1, tile, block_agg, status);
     __syncthreads();
     return block_excl + warp_tot[wid] + (incl - tsum);
 }
@@ -598,21 +613,23 @@ __device__ __forceinline__ int scan_ticket(unsigned long long *state) {
 }
 
 // In-place exclusive scan of n counters.
-__global__ void __launch_bounds__(kScanThreads) k_scan_counts(unsigned *__restrict__ data, size_t n,
-                                                              unsigned long long *state, int *status) {
+__global__ void __launch_bounds__(kCellScanThreads) k_scan_counts(unsigned *__restrict__ data, size_t n,
+                                                                  unsigned long long *state, int *status) {
+    constexpr int ITEMS = kCellScanItems;
     const int tile = scan_ticket(state);
-    const size_t base = static_cast<size_t>(tile) * kScanTile + static_cast<size_t>(threadIdx.x) * kScanItems;
-    unsigned v[kScanItems];
-    if (base + kScanItems <= n) {
+    const size_t base = static_cast<size_t>(tile) * (kCellScanThreads * ITEMS) +
+                        static_cast<size_t>(threadIdx.x) * ITEMS;
+    unsigned v[ITEMS];
+    if (base + ITEMS <= n) {
         const uint4 a = *reinterpret_cast<const uint4 *>(data + base);
         const uint4 b = *reinterpret_cast<const uint4 *>(data + base + 4);
         v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
     } else {
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? data[base + k] : 0u;
+        for (int k = 0; k < ITEMS; ++k) v[k] = base + k < n ? data[base + k] : 0u;
     }
-    unsigned run = block_scan_lookback(v, tile, state, status);
-    if (base + kScanItems <= n) {
+    unsigned run = block_scan_lookback<kCellScanThreads, ITEMS>(v, tile, state, status);
+    if (base + ITEMS <= n) {
         uint4 a, b;
         a.x = run, run += v[0], a.y = run, run += v[1], a.z = run, run += v[2], a.w = run, run += v[3];
         b.x = run, run += v[4], b.y = run, run += v[5], b.z = run, run += v[6], b.w = run;
@@ -620,7 +637,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_counts(unsigned *__restri
         *reinterpret_cast<uint4 *>(data + base + 4) = b;
     } else {
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
+        for (int k = 0; k < ITEMS; ++k)
             if (base + k < n) {
                 data[base + k] = run;
                 run += v[k];
@@ -632,38 +649,26 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_counts(unsigned *__restri
 // t * cells_per_tile) holds ceil(count / chunk) items of up to `chunk`
 // points.  One scan over the per-tile item counts places every tile's items;
 // the thread owning index ntiles stores the total in status[0].
-__global__ void __launch_bounds__(kScanThreads, 1) k_scan_emit_chunks(const unsigned *__restrict__ cell_start, int ntiles,
-                                                                   int cells_per_tile, int chunk,
-                                                                   int4 *__restrict__ chunks,
-                                                                   unsigned long long *state, int *status) {
+__global__ void __launch_bounds__(kItemScanThreads, 1) k_scan_emit_chunks(const unsigned *__restrict__ cell_start,
+                                                                       int ntiles, int cells_per_tile, int chunk,
+                                                                       int4 *__restrict__ chunks,
+                                                                       unsigned long long *state, int *status) {
+    static_assert(kItemScanItems == 1, "one bin tile per thread");
     const int tile = scan_ticket(state);
-    const long long base = static_cast<long long>(tile) * kScanTile + static_cast<long long>(threadIdx.x) * kScanItems;
-    unsigned v[kScanItems];
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        const long long t = base + k;
-        v[k] = 0u;
-        if (t < ntiles) {
-            const unsigned cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] -
-                                 cell_start[static_cast<size_t>(t) * cells_per_tile];
-            v[k] = (cnt + chunk - 1) / chunk;
-        }
+    const long long t = static_cast<long long>(tile) * kItemScanThreads + threadIdx.x;  // bin tile
+    unsigned start = 0, cnt = 0;
+    unsigned v[1] = {0u};
+    if (t < ntiles) {
+        start = cell_start[static_cast<size_t>(t) * cells_per_tile];
+        cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] - start;
+        v[0] = (cnt + chunk - 1) / chunk;
     }
-    unsigned run = block_scan_lookback(v, tile, state, status);
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        const long long t = base + k;
-        if (t == ntiles) status[0] = static_cast<int>(run);
-        if (v[k]) {
-            const unsigned start = cell_start[static_cast<size_t>(t) * cells_per_tile];
-            const unsigned cnt = cell_start[static_cast<size_t>(t + 1) * cells_per_tile] - start;
-            for (unsigned c = 0; c < v[k]; ++c) {
-                const unsigned off = c * chunk;
-                chunks[run + c] = make_int4(static_cast<int>(t), static_cast<int>(start + off),
-                                            static_cast<int>(min(cnt - off, static_cast<unsigned>(chunk))), 0);
-            }
-        }
-        run += v[k];
+    const unsigned run = block_scan_lookback<kItemScanThreads, 1>(v, tile, state, status);
+    if (t == ntiles) status[0] = static_cast<int>(run);
+    for (unsigned c = 0; c < v[0]; ++c) {
+        const unsigned off = c * chunk;
+        chunks[run + c] = make_int4(static_cast<int>(t), static_cast<int>(start + off),
+                                    static_cast<int>(min(cnt - off, static_cast<unsigned>(chunk))), 0);
     }
 }
 
@@ -799,7 +804,8 @@ int setup_bins(nfft2d_plan_s *p) {
     p->ncells = static_cast<size_t>(g.tiles1) * g.tiles2 * g.T * g.T;
     const size_t ntiles = static_cast<size_t>(g.tiles1) * g.tiles2;
     // two 64-bit scan states (cells, work items), counted in 32-bit words
-    p->scan_tmp_elems = 2 * (scan_state_words(p->ncells + 1) + scan_state_words(ntiles + 1));
+    p->scan_tmp_elems = 2 * (scan_state_words(p->ncells + 1, kCellScanThreads * kCellScanItems) +
+                             scan_state_words(ntiles + 1, kItemScanThreads * kItemScanItems));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->cell_count), sizeof(unsigned) * (p->ncells + 1)));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->scan_tmp), sizeof(unsigned) * p->scan_tmp_elems));
     return NFFT2D_OK;
@@ -1337,8 +1343,9 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     const int blocks = (Mi + 255) / 256;
     // ticket + tile words of the cell scan, then of the work-item scan
     unsigned long long *scan_state = reinterpret_cast<unsigned long long *>(p->scan_tmp);
-    const int scan_words = static_cast<int>(scan_state_words(p->ncells + 1) +
-                                            scan_state_words(static_cast<size_t>(g.tiles1) * g.tiles2 + 1));
+    constexpr int kCellTile = kCellScanThreads * kCellScanItems, kItemTile = kItemScanThreads * kItemScanItems;
+    const int scan_words = static_cast<int>(scan_state_words(p->ncells + 1, kCellTile) +
+                                            scan_state_words(static_cast<size_t>(g.tiles1) * g.tiles2 + 1, kItemTile));
     if (p->precision == NFFT2D_F64) {
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec64><<<blocks, 256, 0, p->stream>>>(
@@ -1360,7 +1367,7 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     }
     NFFT_TRY_CUDA(cudaGetLastError());
     const size_t cells_n = p->ncells + 1;
-    k_scan_counts<<<static_cast<unsigned>((cells_n + kScanTile - 1) / kScanTile), kScanThreads, 0, p->stream>>>(
+    k_scan_counts<<<static_cast<unsigned>((cells_n + kCellTile - 1) / kCellTile), kCellScanThreads, 0, p->stream>>>(
         p->cell_count, cells_n, scan_state, p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
     if (p->precision == NFFT2D_F64)
@@ -1371,9 +1378,9 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
                                                             p->cell_count, Mi, static_cast<Rec32 *>(p->recs));
     NFFT_TRY_CUDA(cudaGetLastError());
     const int ntiles = g.tiles1 * g.tiles2;
-    k_scan_emit_chunks<<<static_cast<unsigned>((ntiles + 1 + kScanTile - 1) / kScanTile), kScanThreads, 0,
+    k_scan_emit_chunks<<<static_cast<unsigned>((ntiles + 1 + kItemTile - 1) / kItemTile), kItemScanThreads, 0,
                          p->stream>>>(p->cell_count, ntiles, g.T * g.T, p->chunk, p->chunks,
-                                      scan_state + scan_state_words(cells_n), p->d_status);
+                                      scan_state + scan_state_words(cells_n, kCellTile), p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
     stage_end(p, ST_SORT);
     if (async) {

@@ -69,7 +69,10 @@ extern "C" {
 #define NFFT2D_UNITS_UNIT    1  /* period 1, [-0.5, 0.5)                   */
 #define NFFT2D_UNITS_RADIANS 2  /* period 2*pi, [-pi, pi)                  */
 
-/* Kernel variants for the gather (type 2) and the spread (type 1). */
+/* Kernel variants for the gather (type 2) and the spread (type 1).  AUTO:
+ * FP32 spreads are TILED; the FP32 gather is chosen at set_points from the
+ * bin density (DIRECT from 128 points per 16 x 16 tile up, else TILED);
+ * FP64 uses DIRECT. */
 #define NFFT2D_VARIANT_AUTO   0
 #define NFFT2D_VARIANT_TILED  1  /* binned tiles staged by TMA in shared memory */
 #define NFFT2D_VARIANT_DIRECT 2  /* sorted points, taps read straight from L2   */

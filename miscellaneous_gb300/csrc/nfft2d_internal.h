@@ -91,6 +91,7 @@ struct nfft2d_plan_s {
     nfft2d::WinPoly poly{};      // FP32 window polynomials
     int chunk = 256;
     int gather_variant = NFFT2D_VARIANT_TILED;
+    bool gather_auto = true;     // FP32: pick the gather by bin density at set_points
     int spread_variant = NFFT2D_VARIANT_TILED;
     int compensated = 1;
     int device = 0;

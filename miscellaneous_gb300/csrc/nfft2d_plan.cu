@@ -160,6 +160,16 @@ bool use_fused(const nfft2d_plan_s *p) {
     return p->fft_mode < 0 && 1LL * p->g.n1 * p->g.n2 < 2048LL * 2048LL;
 }
 
+// The automatic FP32 gather: the TMA-tiled patches while the bins are thin,
+// the direct 16-byte-load gather from 128 points per 16 x 16 tile up (the
+// autotuner's picks on GB300: tiled at 64 points per tile -- 64^2
+// coefficients, 4096 points --, direct at 256 -- the polar raster, uniform
+// and clustered 2^20..2^24 sets; the direct gather is 13 % faster there).
+int auto_gather(const nfft2d_plan_s *p, long long M) {
+    const long long tiles = static_cast<long long>(p->g.tiles1) * p->g.tiles2;
+    return M >= 128 * tiles ? NFFT2D_VARIANT_DIRECT : NFFT2D_VARIANT_TILED;
+}
+
 int fft_mode_in_use(const nfft2d_plan_s *p) {
     if (use_fused(p)) return 2;
     const bool pruned = p->fft_mode == 1 || (p->fft_mode < 0 && 1LL * p->g.n1 * p->g.n2 >= 2048LL * 2048LL);
@@ -1105,6 +1115,7 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     if (precision == NFFT2D_F64) {
         p->gather_variant = NFFT2D_VARIANT_DIRECT;
         p->spread_variant = NFFT2D_VARIANT_DIRECT;
+        p->gather_auto = false;
     }
     auto fail = [&](int s) {
         destroy_plan(p);
@@ -1214,11 +1225,14 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     for (int v : {t->gather_variant, t->spread_variant})
         if (v < NFFT2D_VARIANT_AUTO || v > NFFT2D_VARIANT_DIRECT) return NFFT2D_ERR_INVALID_ARG;
     const int auto_v = p->precision == NFFT2D_F32 ? NFFT2D_VARIANT_TILED : NFFT2D_VARIANT_DIRECT;
-    const int gv = t->gather_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->gather_variant;
+    const bool gauto = t->gather_variant == NFFT2D_VARIANT_AUTO && p->precision == NFFT2D_F32;
+    const int gv = gauto ? auto_gather(p, p->points_valid ? p->M : 0)
+                         : (t->gather_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->gather_variant);
     const int sv = t->spread_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->spread_variant;
     if (p->precision == NFFT2D_F64 && (gv == NFFT2D_VARIANT_TILED || sv == NFFT2D_VARIANT_TILED))
         return NFFT2D_ERR_UNSUPPORTED;
     p->gather_variant = gv;
+    p->gather_auto = gauto;
     p->spread_variant = sv;
     if (t->compensated >= 0) p->compensated = t->compensated ? 1 : 0;
     if (t->fft_mode > 2 || t->fft_mode < -1) return NFFT2D_ERR_INVALID_ARG;
@@ -1383,6 +1397,7 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
                                       scan_state + scan_state_words(cells_n, kCellTile), p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
     stage_end(p, ST_SORT);
+    if (p->gather_auto) p->gather_variant = auto_gather(p, M);
     if (async) {
         // the work-item count stays on the device (status[0]); the kernels
         // read it there, nfft2d_synchronize fetches it and reports errors

@@ -69,3 +69,21 @@ def test_async_nonfinite_reported_by_synchronize():
         ref = p.forward(F)
         p.synchronize()
     torch.testing.assert_close(out, ref, rtol=0, atol=0)
+
+
+def test_automatic_gather_follows_bin_density():
+    """The automatic FP32 gather is the tiled one on thin bins and the direct
+    one from 128 points per 16 x 16 tile up, decided at set_points."""
+    from miscellaneous_gb300.nfft import Plan
+    N = 64  # 128^2 cells, 64 tiles
+    with Plan(N, N) as p:
+        x1, x2, _, _ = _inputs(4096, N, seed=1)       # 64 points per tile
+        p.set_points(x1, x2)
+        assert p.info()["gather_variant"] == 1
+        x1, x2, _, _ = _inputs(64 * 256, N, seed=2)   # 256 points per tile
+        p.set_points(x1, x2, sync=False)
+        assert p.info()["gather_variant"] == 2
+        p.set_tuning(gather_variant=1)                # an explicit choice sticks
+        p.set_points(x1, x2)
+        assert p.info()["gather_variant"] == 1
+        p.synchronize()

@@ -119,16 +119,20 @@ def test_uncompensated_gather_still_within_bar(orc):
     assert orc.rel_l2(fwd, orc.ndft_type2(F, _grid(x1, 64), _grid(x2, 64), sign=-1)) < 1e-5
 
 
-@pytest.mark.parametrize("N1,N2,sigma", [(22, 22, 2.0), (8, 8, 2.0), (16, 64, 2.0), (64, 64, 1.5), (48, 24, 1.25)])
+@pytest.mark.parametrize("N1,N2,sigma", [(22, 22, 2.0), (8, 8, 2.0), (16, 64, 2.0), (64, 64, 1.5), (48, 24, 1.25),
+                                         (40, 80, 1.6), (96, 48, 4 / 3)])
 def test_odd_shapes_and_oversampling(orc, N1, N2, sigma):
-    """FP32 vs the restated algorithm: 2e-6 at sigma >= 1.5.  At sigma = 1.25
+    """FP32 vs the restated algorithm: 2e-6 at sigma >= 1.5.  (40, 80, 1.6) and
+    (96, 48, 4/3) land on power-of-two grids (64 x 128, 128 x 64), so the fused
+    FFT passes run with band widths that are not multiples of the columns per
+    CTA.  At sigma = 1.25
     (K = 5) the deapodization table spans I0(K alpha)/I0(K sqrt(alpha^2 -
     (pi/sigma)^2)) = I0(18.8)/I0(14.0) ~ 92x across the band, which scales
     FP32 rounding at the band edges by the same factor, so the bar there is 1e-4."""
     F, x1, x2, f = _inputs(N1, N2, 900, seed=N1 + N2)
     fwd, adj, sref, _ = _run({"sigma": sigma, "K": 5}, F, x1, x2, f)
     g1, g2 = _grid(x1, N1), _grid(x2, N2)
-    tol = 2e-6 if sigma >= 1.5 else 1e-4
+    tol = 2e-6 if sigma >= 1.5 else 1e-4  # sigma = 4/3: the deapodization spans ~46x across the band
     assert orc.rel_l2(fwd, orc.nfft1_2d(F, g1, g2, c=sigma, K=5, sign=-1)) < tol
     assert orc.rel_l2(sref, orc.nfft2_2d(f, g1, g2, N1, N2, c=sigma, K=5, sign=-1)) < tol
     assert orc.rel_l2(adj, orc.nfft2_2d(f, g1, g2, N1, N2, c=sigma, K=5, sign=+1)) < tol

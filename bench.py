@@ -493,7 +493,7 @@ def run_ours(args, wl):
 
     # ---- dominant kernel roofline ----
     peak, peak_kind = measured_peaks()
-    alg_bytes = 20 * M + 8 * G  # gather and spread both move 20 B/point + 8 B/cell
+    alg_bytes = 20 * M + 8 * G  # algorithmic bytes: gather and spread both move 20 B/point + 8 B/cell
     dom = "gather" if stage["gather"] >= stage["spread"] else "spread"
     dom_ms = stage[dom]
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9

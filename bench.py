@@ -311,6 +311,24 @@ def rel_l2(a, b, torch):
     return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
 
 
+def subset_accuracy(f_fwd, F, f, x1, x2, N1, N2, nsub, seed, plan_kw, stream, torch):
+    """Rel-L2 of a forward result f_fwd (all points) against the FP64 NDFT on
+    a random subset of the points, and of the adjoint of f over that subset
+    (a plan on the subset) against the FP64 type-1 sum."""
+    from miscellaneous_gb300.nfft import Plan
+    M = x1.numel()
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    idx = torch.randperm(M, generator=g)[:min(M, nsub)].to(x1.device)
+    e_fwd = rel_l2(f_fwd[idx], ndft_type2_subset(F.reshape(N1, N2), x1, x2, idx, -1, torch), torch)
+    sub_plan = Plan(N1, N2, precision="f32", stream=stream, **plan_kw)
+    sub_plan.set_points(x1[idx].contiguous(), x2[idx].contiguous(), units="unit")
+    fa = sub_plan.adjoint(f[idx].contiguous())
+    sub_plan.synchronize()
+    e_adj = rel_l2(fa, ndft_type1(f[idx], x1[idx], x2[idx], N1, N2, +1, torch), torch)
+    sub_plan.close()
+    return e_fwd, e_adj, int(idx.numel()), idx
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline (oracle restatement of the reference algorithm)
 # ---------------------------------------------------------------------------
@@ -576,21 +594,44 @@ def run_ours(args, wl):
     if not args.no_accuracy and rank == 0:
         plan.forward(F, out=f_out)
         plan.synchronize()
-        g = torch.Generator(device="cpu").manual_seed(7)
-        nsub = min(M, 65536)
-        idx = torch.randperm(M, generator=g)[:nsub].to(dev)
-        Fm = F.reshape(N1, N2)
-        ref = ndft_type2_subset(Fm, x1, x2, idx, -1, torch)
-        e_fwd = rel_l2(f_out[idx], ref, torch)
-        # adjoint on the same subset of points (type 1 over the subset)
-        sub_plan = Plan(N1, N2, sigma=wl["sigma"], K=wl["K"], precision="f32", stream=stream)
-        sub_plan.set_points(x1[idx].contiguous(), x2[idx].contiguous(), units="unit")
-        fa = sub_plan.adjoint(f[idx].contiguous())
-        sub_plan.synchronize()
-        e_adj = rel_l2(fa, ndft_type1(f[idx], x1[idx], x2[idx], N1, N2, +1, torch), torch)
-        sub_plan.close()
+        e_fwd, e_adj, nsub, _ = subset_accuracy(f_out, F, f, x1, x2, N1, N2, 65536, 7,
+                                                {"sigma": wl["sigma"], "K": wl["K"]}, stream, torch)
         accuracy = {"rel_l2_forward": e_fwd, "rel_l2_adjoint": e_adj, "subset_points": nsub,
                     "oracle": "FP64 NDFT (exact phase reduction) via torch complex128 on the GPU"}
+
+    # ---- set_points on its own, and "set_points + execute" (after timing) ----
+    plan.enable_timing(True)
+    sp_ms = []
+    for r in range(args.warmup + args.steps):
+        flush.zero_()
+        plan.set_points(x1, x2, units="unit")
+        if r >= args.warmup:
+            sp_ms.append(plan.timings()["sort_ms"])
+    set_points_ms = sum(sp_ms) / len(sp_ms)
+
+    # ---- cuFFT, timed on its own on the same grid (a second plan in cuFFT mode) ----
+    cufft = None
+    if plan.info()["fft_mode"] == 2:
+        cplan = Plan(N1, N2, sigma=wl["sigma"], K=wl["K"], precision="f32", stream=stream)
+        cplan.set_tuning(fft_mode=0)
+        cplan.set_points(x1, x2, units="unit")
+        cplan.enable_timing(True)
+        ts = []
+        for r in range(args.warmup + args.steps):
+            cplan.forward(F, out=f_out)
+            cplan.adjoint(f, out=F_out)
+            if r >= args.warmup:
+                ts.append(cplan.timings())
+            flush.zero_()
+        cplan.synchronize()
+        cplan.close()
+        avg = {k: sum(t[k] for t in ts) / len(ts) for k in ("pad_ms", "fft_type2_ms", "halo_fill_ms", "fold_ms",
+                                                            "fft_type1_ms", "crop_ms")}
+        cufft = {"fft_fwd_ms": avg["fft_type2_ms"], "fft_adj_ms": avg["fft_type1_ms"],
+                 "fft_ms": avg["fft_type2_ms"] + avg["fft_type1_ms"],
+                 "with_pad_fill_fold_crop_ms": sum(avg.values()),
+                 "note": "cuFFT 2D plan on the same grid with the separate pad / halo fill / halo fold / crop "
+                         "kernels; the line's own FFT is the fused passes"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -612,6 +653,11 @@ def run_ours(args, wl):
             "adjoint_ms": stage["spread"] + stage["fold"] + stage["fft_adj"] + stage["crop"],
             "fft_ms": (stage["pad"] + stage["fft_fwd"] + stage["fold"] + stage["fft_adj"]) if fused
             else stage["fft_fwd"] + stage["fft_adj"],
+            "cufft_separate": cufft,
+            "set_points_ms": set_points_ms,
+            "set_points_plus_execute": {"value": world * M / ((t_step + set_points_ms) * 1e-3), "unit": UNIT,
+                                        "ms_per_step": t_step + set_points_ms,
+                                        "note": "binning timed by the plan's events, plus one execute step"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
             "gpu_launches": 6 * args.steps,
             "gpu_launches_note": ("our kernels in the timed region per step: column FFT+pad, row FFT+fill, gather, "
@@ -679,12 +725,34 @@ def run_lsq(args, wl):
     plan.forward(F - t_ls * gF, out=r)
     loss1 = float(torch.sum(torch.abs(r - y) ** 2))
     plan.synchronize()
+    # accuracy against FP64 sums on a 65,536-point subset: forward, adjoint,
+    # and the coordinate gradient (v = 2 r; df/dx1 = sum_k F_k (-2 pi i k1) e_k(x))
+    accuracy = None
+    if not args.no_accuracy:
+        f_fwd = plan.forward(F)
+        v = 2.0 * (f_fwd - y)
+        g1, g2 = plan.grad_x(F, v)
+        plan.synchronize()
+        e_fwd, e_adj, nsub, idx = subset_accuracy(f_fwd, F, v, x1, x2, N1, N2, 65536, 11,
+                                                  {"sigma": wl["sigma"], "K": wl["K"]}, stream, torch)
+        Fm = F.reshape(N1, N2).to(torch.complex128)
+        k1 = (torch.arange(N1, device=dev, dtype=torch.float64) - N1 // 2)[:, None]
+        k2 = (torch.arange(N2, device=dev, dtype=torch.float64) - N2 // 2)[None, :]
+        d1 = ndft_type2_subset(Fm * (-2j * math.pi) * k1, x1, x2, idx, -1, torch)
+        d2 = ndft_type2_subset(Fm * (-2j * math.pi) * k2, x1, x2, idx, -1, torch)
+        vs = v[idx].to(torch.complex128)
+        r1, r2 = torch.real(vs.conj() * d1), torch.real(vs.conj() * d2)
+        e_grad = float(torch.linalg.vector_norm(torch.cat([g1[idx].double() - r1, g2[idx].double() - r2])) /
+                       torch.linalg.vector_norm(torch.cat([r1, r2])))
+        accuracy = {"rel_l2_forward": e_fwd, "rel_l2_adjoint": e_adj, "rel_l2_grad_x": e_grad,
+                    "subset_points": nsub,
+                    "oracle": "FP64 NDFT and its coordinate derivative via torch complex128 on the GPU"}
     line = {"metric": METRIC, "value": M / (t * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(wl["config"], l2="256 MB buffer written between timed steps",
                            step="forward + residual + adjoint (dL/df) + coordinate gradient (dL/dx)"),
-            "loss_before": loss0, "loss_after_one_step": loss1, "clocks": clocks.summary()}
+            "loss_before": loss0, "loss_after_one_step": loss1, "accuracy": accuracy, "clocks": clocks.summary()}
     print(json.dumps(line))
     plan.close()
 
@@ -923,13 +991,39 @@ def run_batch(args, wl):
 
     t_seq = timed(sequential)
     batch.synchronize()
+    accuracy = None
+    if not args.no_accuracy:
+        # the batched results themselves: forward on point subsets of a few
+        # transforms, adjoint of the transforms with the fewest points
+        # against the full FP64 type-1 sum
+        batched()
+        batch.synchronize()
+        order = sorted(range(len(sizes)), key=lambda t: wl["items"][t]["M"])
+        fwd_ts = sorted(set([order[0], order[len(order) // 2], order[-1], len(order) // 3]))
+        e_fwd = 0.0
+        for t in fwd_ts:
+            n1, n2 = sizes[t]
+            gsub = torch.Generator(device="cpu").manual_seed(100 + t)
+            idx = torch.randperm(x1s[t].numel(), generator=gsub)[:16384].to(dev)
+            ref = ndft_type2_subset(Fs[t].reshape(n1, n2), x1s[t], x2s[t], idx, -1, torch)
+            e_fwd = max(e_fwd, rel_l2(f_out[t][idx], ref, torch))
+        adj_ts = [t for t in order if wl["items"][t]["M"] * sizes[t][0] * sizes[t][1] <= 4e10][:3]
+        e_adj = 0.0
+        for t in adj_ts:
+            n1, n2 = sizes[t]
+            ref = ndft_type1(fs[t], x1s[t], x2s[t], n1, n2, +1, torch)
+            e_adj = max(e_adj, rel_l2(F_out[t], ref, torch))
+        accuracy = {"rel_l2_forward_max": e_fwd, "forward_transforms": fwd_ts, "forward_subset_points": "min(M, 16384)",
+                    "rel_l2_adjoint_max": e_adj, "adjoint_transforms": adj_ts,
+                    "oracle": "FP64 NDFT via torch complex128 on the GPU (adjoint: all points of the transform)"}
     line = {"metric": METRIC, "value": total / (t_batch * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_batch, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(wl["config"], l2="256 MB buffer written between timed steps"),
             "sequential_ms_per_step": t_seq, "batched_speedup": t_seq / t_batch,
             "sequential": "one forward + one adjoint per transform through pre-created single-transform plans",
-            "batched": "nfft2d_batch_forward + nfft2d_batch_adjoint, stage sequence replayed as a CUDA graph"}
+            "batched": "nfft2d_batch_forward + nfft2d_batch_adjoint, stage sequence replayed as a CUDA graph",
+            "accuracy": accuracy}
     print(json.dumps(line))
     for p in plans:
         p.close()

@@ -70,8 +70,8 @@ extern "C" {
 #define NFFT2D_UNITS_RADIANS 2  /* period 2*pi, [-pi, pi)                  */
 
 /* Kernel variants for the gather (type 2) and the spread (type 1).  AUTO:
- * FP32 spreads are TILED; the FP32 gather is chosen at set_points from the
- * bin density (DIRECT from 128 points per 16 x 16 tile up, else TILED);
+ * FP32 spreads are TILED; the FP32 gather is chosen at set_points (DIRECT
+ * from 128 points per 16 x 16 tile or 2^18 points up, else TILED);
  * FP64 uses DIRECT. */
 #define NFFT2D_VARIANT_AUTO   0
 #define NFFT2D_VARIANT_TILED  1  /* binned tiles staged by TMA in shared memory */

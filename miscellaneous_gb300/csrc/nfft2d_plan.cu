@@ -160,14 +160,15 @@ bool use_fused(const nfft2d_plan_s *p) {
     return p->fft_mode < 0 && 1LL * p->g.n1 * p->g.n2 < 2048LL * 2048LL;
 }
 
-// The automatic FP32 gather: the TMA-tiled patches while the bins are thin,
-// the direct 16-byte-load gather from 128 points per 16 x 16 tile up (the
-// autotuner's picks on GB300: tiled at 64 points per tile -- 64^2
-// coefficients, 4096 points --, direct at 256 -- the polar raster, uniform
-// and clustered 2^20..2^24 sets; the direct gather is 13 % faster there).
+// The automatic FP32 gather: the direct 16-byte-load gather from 128 points
+// per 16 x 16 tile or 2^18 points up, the TMA-tiled patches for small, thin
+// point sets.  Measured on GB300: tiled for 4096 points on 64^2
+// coefficients (the autotuner's pick, 64 points per tile); direct 13 %
+// faster at 256 points per tile (polar raster, uniform and clustered sets)
+// and 16 % faster for the Knab regridding's 4 M outputs at 64 per tile.
 int auto_gather(const nfft2d_plan_s *p, long long M) {
     const long long tiles = static_cast<long long>(p->g.tiles1) * p->g.tiles2;
-    return M >= 128 * tiles ? NFFT2D_VARIANT_DIRECT : NFFT2D_VARIANT_TILED;
+    return (M >= 128 * tiles || M >= (1LL << 18)) ? NFFT2D_VARIANT_DIRECT : NFFT2D_VARIANT_TILED;
 }
 
 int fft_mode_in_use(const nfft2d_plan_s *p) {

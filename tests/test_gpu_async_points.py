@@ -72,8 +72,9 @@ def test_async_nonfinite_reported_by_synchronize():
 
 
 def test_automatic_gather_follows_bin_density():
-    """The automatic FP32 gather is the tiled one on thin bins and the direct
-    one from 128 points per 16 x 16 tile up, decided at set_points."""
+    """The automatic FP32 gather is the tiled one on small, thin point sets
+    and the direct one from 128 points per 16 x 16 tile (or 2^18 points) up,
+    decided at set_points."""
     from miscellaneous_gb300.nfft import Plan
     N = 64  # 128^2 cells, 64 tiles
     with Plan(N, N) as p:

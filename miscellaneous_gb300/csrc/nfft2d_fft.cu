@@ -32,6 +32,11 @@
 // sequence q at i * P + q, so a warp's global accesses cover P adjacent
 // columns of consecutive rows), row passes keep them contiguous; shared
 // memory indices carry one pad element per 16.
+//
+// The plan uses these passes by default below 2048 x 2048 oversampled cells
+// (nfft2d_plan.cu, use_fused).  From there up a row of 2048 or 4096 points
+// needs 128 or 256 threads at ~115 registers, two CTAs per SM, and cuFFT's
+// pruned passes are faster (4096^2: 292 vs 421 us for both directions).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -467,10 +472,9 @@ FftArgs fft_args(const nfft2d_plan_s *p, int sign) {
     return a;
 }
 
+// Dynamic shared memory above the 48 KB default needs an opt-in per kernel.
 template <typename KernelT>
-cudaError_t launch_fft_kernel(KernelT kernel, int blocks, int smem, cudaStream_t st) {
-    (void)blocks;
-    (void)st;
+cudaError_t allow_smem(KernelT kernel, int smem) {
     if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     return cudaSuccess;
 }
@@ -511,7 +515,7 @@ cudaError_t fused_type2_cols(const nfft2d_plan_s *p, int sign, const void *F) {
     const int blocks = (p->N2 + (1 << a.logP) - 1) >> a.logP;
     const int threads = (a.n1 << a.logP) / 16;
     const int smem = padded_elems(a.n1 << a.logP) * static_cast<int>(sizeof(float2));
-    cudaError_t e = launch_fft_kernel(k_fft_cols_pad, blocks, smem, p->stream);
+    cudaError_t e = allow_smem(k_fft_cols_pad, smem);
     if (e != cudaSuccess) return e;
     k_fft_cols_pad<<<blocks, threads, smem, p->stream>>>(
         static_cast<const float2 *>(F), static_cast<float2 *>(p->grid), static_cast<const float *>(p->deap1),
@@ -525,7 +529,7 @@ cudaError_t fused_type2_rows(const nfft2d_plan_s *p, int sign) {
     const int blocks = a.n1 >> a.logP;
     const int threads = (a.n2 << a.logP) / 16;
     const int smem = padded_elems(a.n2 << a.logP) * static_cast<int>(sizeof(float2));
-    cudaError_t e = launch_fft_kernel(k_fft_rows_fill, blocks, smem, p->stream);
+    cudaError_t e = allow_smem(k_fft_rows_fill, smem);
     if (e != cudaSuccess) return e;
     k_fft_rows_fill<<<blocks, threads, smem, p->stream>>>(static_cast<float2 *>(p->grid), p->tw2, a);
     return cudaGetLastError();
@@ -537,7 +541,7 @@ cudaError_t fused_type1_rows(const nfft2d_plan_s *p, int sign) {
     const int blocks = a.n1 >> a.logP;
     const int threads = (a.n2 << a.logP) / 16;
     const int smem = padded_elems(a.n2 << a.logP) * static_cast<int>(sizeof(float2));
-    cudaError_t e = launch_fft_kernel(k_fft_rows_fold, blocks, smem, p->stream);
+    cudaError_t e = allow_smem(k_fft_rows_fold, smem);
     if (e != cudaSuccess) return e;
     k_fft_rows_fold<<<blocks, threads, smem, p->stream>>>(static_cast<float2 *>(p->grid), p->tw2, a);
     return cudaGetLastError();
@@ -549,7 +553,7 @@ cudaError_t fused_type1_cols(const nfft2d_plan_s *p, int sign, void *F) {
     const int blocks = (p->N2 + (1 << a.logP) - 1) >> a.logP;
     const int threads = (a.n1 << a.logP) / 16;
     const int smem = padded_elems(a.n1 << a.logP) * static_cast<int>(sizeof(float2));
-    cudaError_t e = launch_fft_kernel(k_fft_cols_crop, blocks, smem, p->stream);
+    cudaError_t e = allow_smem(k_fft_cols_crop, smem);
     if (e != cudaSuccess) return e;
     k_fft_cols_crop<<<blocks, threads, smem, p->stream>>>(
         static_cast<const float2 *>(p->grid), static_cast<float2 *>(F), static_cast<const float *>(p->deap1),

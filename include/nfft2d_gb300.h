@@ -220,8 +220,8 @@ int nfft2d_ndft2d_f64(const double *X, const double *Y, const double *u, const d
 /* ---- batches: many transforms of uneven size in one go ------------------
  * No reference counterpart: the reference runs one NFFT2_2D_GPU per PSO
  * particle in a host loop (Synthesis/PSO/PSO.cu:348, Synthesis.cu:395).
- * A batch holds `count` FP32 transforms (N1[t] x N2[t], shared sigma and K,
- * 16 x 16 tiles).  Grids of equal size share one batched cuFFT plan; every
+ * A batch holds `count` FP32 transforms (N1[t] x N2[t], shared sigma and K
+ * -- or a K per transform with nfft2d_batch_create_k --, 16 x 16 tiles).  Grids of equal size share one batched cuFFT plan; every
  * other stage covers all transforms with one launch (a gather with one
  * thread per binned point of all transforms, a persistent spread over the
  * work items of all transforms); the stage sequence
@@ -233,6 +233,13 @@ int nfft2d_ndft2d_f64(const double *X, const double *Y, const double *u, const d
 typedef struct nfft2d_batch_s *nfft2d_batch;
 int nfft2d_batch_create(nfft2d_batch *batch, int count, const int *N1, const int *N2, double sigma, int K,
                         void *stream);
+/* As nfft2d_batch_create with a window half-width per transform (K[t], 2 to
+ * 8; uneven N and K in one batch).  Transforms are grouped internally by K:
+ * the gather and the spread run once per distinct K, every other stage
+ * once for the whole batch.  All other calls keep the caller's transform
+ * order. */
+int nfft2d_batch_create_k(nfft2d_batch *batch, int count, const int *N1, const int *N2, const int *K, double sigma,
+                          void *stream);
 int nfft2d_batch_destroy(nfft2d_batch batch);
 int nfft2d_batch_set_points(nfft2d_batch batch, const long long *M, const void *const *x1, const void *const *x2,
                             int coord_dtype, int units);

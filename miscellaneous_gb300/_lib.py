@@ -114,6 +114,7 @@ _SIGNATURES = {
     "nfft2d_ndft2d_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _LL, _LL, _I, _P]),
     "nfft2d_forward_small_noalloc": (_I, [_I, _I, _I, _LL, _P, _P, _I, _P, _P, _P]),
     "nfft2d_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _P, _D, _I, _P]),
+    "nfft2d_batch_create_k": (_I, [ctypes.POINTER(_P), _I, _P, _P, _P, _D, _P]),
     "nfft2d_batch_destroy": (_I, [_P]),
     "nfft2d_batch_set_points": (_I, [_P, _P, _P, _P, _I, _I]),
     "nfft2d_batch_forward": (_I, [_P, _P, _P]),

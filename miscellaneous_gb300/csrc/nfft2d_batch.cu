@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <new>
 #include <vector>
 
@@ -195,13 +196,15 @@ __global__ void k_batch_fold(const BatchDesc *__restrict__ d) {
 // Direct gather over all transforms: one thread per binned point, the
 // transform found by its global point index; taps read straight from that
 // transform's padded grid (the single-plan FP32 direct gather).
+// One launch per window width: transforms [first, first + n) of the batch's
+// internal order share K and hold global points [point0, point0 + npoints).
 template <int K>
 __global__ void __launch_bounds__(kThreads)
-    k_batch_gather_direct(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total_points,
-                          const __grid_constant__ WinPoly wp, int *status) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= total_points) return;
-    const int t = find_transform<3>(d, n, i);
+    k_batch_gather_direct(const BatchDesc *__restrict__ d, int first, int n, const BatchIO *__restrict__ io,
+                          int point0, int npoints, const __grid_constant__ WinPoly wp, int *status) {
+    const int i = point0 + blockIdx.x * kThreads + threadIdx.x;
+    if (i >= point0 + npoints) return;
+    const int t = first + find_transform<3>(d + first, n, i);
     const BatchDesc &D = d[t];
     const int4 raw = __ldg(reinterpret_cast<const int4 *>(D.recs) + (i - D.point_base));
     const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
@@ -215,10 +218,12 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---- persistent spread over the work items of all transforms --------------
+// One launch per window width: transforms [first, first + n) hold the global
+// work items [chunk0, chunk0 + total).
 template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32)
-    k_batch_spread(const BatchDesc *__restrict__ d, int n, const BatchIO *__restrict__ io, int total, Geom g0,
-                   const __grid_constant__ WinPoly wp, int chunk, int *work, int *status) {
+    k_batch_spread(const BatchDesc *__restrict__ d, int first, int n, const BatchIO *__restrict__ io, int chunk0,
+                   int total, Geom g0, const __grid_constant__ WinPoly wp, int chunk, int *work, int *status) {
     extern __shared__ unsigned char smem_raw[];
     constexpr int PR = kRegTile + 2 * K;
     constexpr int SP = point_scratch<K>();
@@ -234,8 +239,9 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
         if (lane == 0) item = atomicAdd(work, 1);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= total * parts) break;
-        const int gc = item / parts, part = item - gc * parts;
-        const int t = find_transform<0>(d, n, gc);
+        const int gl = item / parts, part = item - gl * parts;
+        const int gc = chunk0 + gl;
+        const int t = first + find_transform<0>(d + first, n, gc);
         const BatchDesc &D = d[t];
         int4 ch = __ldg(&D.chunks[gc - D.chunk_base]);
         const int first = part * kSpreadItem;
@@ -260,15 +266,19 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 // host object
 // ---------------------------------------------------------------------------
 struct nfft2d_batch_s {
-    int count = 0, K = 6;
+    int count = 0;
     double sigma = 2.0;
+    // transforms are kept in an internal order sorted by (K, N1, N2): each
+    // window width and each cuFFT size group is a contiguous range.
+    // order[i] is the caller's index of internal transform i.
+    std::vector<int> order;
     cudaStream_t user_stream = nullptr;
     cudaStream_t stream = nullptr;  // the batch's own stream (captured into graphs)
     std::vector<nfft2d_plan_s *> plans;
     void *grids = nullptr;
     size_t grid_bytes = 0;
     struct Group {
-        int N1, N2;
+        int K, N1, N2;
         std::vector<int> members;  // transform indices, contiguous in `grids`
         size_t first_elem = 0;     // element offset of the first member's grid
         cufftHandle fft = 0;
@@ -286,8 +296,16 @@ struct nfft2d_batch_s {
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // type-2 forward, type-1 adjoint, type-1 sign -1
     cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_io = nullptr;
     bool io_pending = false;
-    Geom g0{};
-    WinPoly poly{};  // window polynomials (shared sigma, K)
+    // transforms [first, first + n) of the internal order share the window
+    // width K: one gather and one spread launch each
+    struct KGroup {
+        int K = 6, first = 0, n = 0;
+        int chunk0 = 0, total_chunks = 0;  // their global work items
+        int point0 = 0, total_points = 0;  // their global points
+        Geom g0{};                         // patch geometry of the width
+        WinPoly poly{};                    // window polynomials of the width
+    };
+    std::vector<KGroup> kgroups;
 };
 
 namespace {
@@ -340,14 +358,70 @@ int run_ffts(nfft2d_batch_s *b, int dir) {
     return NFFT2D_OK;
 }
 
-// type 2: forward (type 2, sign -1); type 1: adjoint (type 1, sign +1);
-// type -1: the reference's spreading NFFT2_2D (type 1, sign -1).
 template <int K>
-int enqueue_stages(nfft2d_batch_s *b, int type) {
+int launch_gather(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg) {
+    if (kg.total_points == 0) return NFFT2D_OK;
+    k_batch_gather_direct<K><<<(kg.total_points + kThreads - 1) / kThreads, kThreads, 0, b->stream>>>(
+        b->d_desc, kg.first, kg.n, b->d_io, kg.point0, kg.total_points, kg.poly, b->d_status);
+    B_TRY(cudaGetLastError());
+    return NFFT2D_OK;
+}
+
+template <int K>
+int launch_spread(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg, int sms) {
+    if (kg.total_chunks == 0) return NFFT2D_OK;
+    const int pstride = patch_stride_elems(kg.g0);
+    const int smem = kSpreadWarps * pstride * static_cast<int>(sizeof(float2)) + 128 +
+                     kSpreadWarps * 32 * point_scratch<K>() * static_cast<int>(sizeof(float));
+    auto kernel = k_batch_spread<K>;
+    if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int per_sm = 0;
+    B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSpreadWarps * 32, smem));
+    const int chunk = b->plans[kg.first]->chunk;
+    const long long items = static_cast<long long>(kg.total_chunks) * ((chunk + kSpreadItem - 1) / kSpreadItem);
+    const int blocks = static_cast<int>(std::max(1LL, std::min<long long>((items + kSpreadWarps - 1) / kSpreadWarps,
+                                                                    std::max(per_sm, 1) * sms)));
+    B_TRY(cudaMemsetAsync(b->d_work, 0, sizeof(int), b->stream));
+    kernel<<<blocks, kSpreadWarps * 32, smem, b->stream>>>(b->d_desc, kg.first, kg.n, b->d_io, kg.chunk0,
+                                                           kg.total_chunks, kg.g0, kg.poly, chunk, b->d_work,
+                                                           b->d_status);
+    B_TRY(cudaGetLastError());
+    return NFFT2D_OK;
+}
+
+int launch_gather_k(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg) {
+    switch (kg.K) {
+        case 2: return launch_gather<2>(b, kg);
+        case 3: return launch_gather<3>(b, kg);
+        case 4: return launch_gather<4>(b, kg);
+        case 5: return launch_gather<5>(b, kg);
+        case 6: return launch_gather<6>(b, kg);
+        case 7: return launch_gather<7>(b, kg);
+        case 8: return launch_gather<8>(b, kg);
+        default: return NFFT2D_ERR_INVALID_ARG;
+    }
+}
+
+int launch_spread_k(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg, int sms) {
+    switch (kg.K) {
+        case 2: return launch_spread<2>(b, kg, sms);
+        case 3: return launch_spread<3>(b, kg, sms);
+        case 4: return launch_spread<4>(b, kg, sms);
+        case 5: return launch_spread<5>(b, kg, sms);
+        case 6: return launch_spread<6>(b, kg, sms);
+        case 7: return launch_spread<7>(b, kg, sms);
+        case 8: return launch_spread<8>(b, kg, sms);
+        default: return NFFT2D_ERR_INVALID_ARG;
+    }
+}
+
+// type 2: forward (type 2, sign -1); type 1: adjoint (type 1, sign +1);
+// type -1: the reference's spreading NFFT2_2D (type 1, sign -1).  The
+// elementwise stages and each size group's FFT cover all transforms at once;
+// the gather and the spread run once per window width.
+int enqueue(nfft2d_batch_s *b, int type) {
     const int n = b->count;
-    const Geom &g0 = b->g0;
-    const int pstride = patch_stride_elems(g0);
-    int per_sm = 0, sms = 0, dev = 0;
+    int sms = 0, dev = 0;
     B_TRY(cudaGetDevice(&dev));
     B_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (type == 2) {
@@ -357,31 +431,16 @@ int enqueue_stages(nfft2d_batch_s *b, int type) {
         if (st != NFFT2D_OK) return st;
         k_batch_fill<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
         B_TRY(cudaGetLastError());
-        if (b->total_points > 0) {
-            k_batch_gather_direct<K><<<(b->total_points + kThreads - 1) / kThreads, kThreads, 0, b->stream>>>(
-                b->d_desc, n, b->d_io, b->total_points, b->poly, b->d_status);
-            B_TRY(cudaGetLastError());
-        }
+        for (const auto &kg : b->kgroups)
+            if ((st = launch_gather_k(b, kg)) != NFFT2D_OK) return st;
     } else {
         B_TRY(cudaMemsetAsync(b->grids, 0, b->grid_bytes, b->stream));
-        if (b->total_chunks > 0) {
-            const int smem = kSpreadWarps * pstride * static_cast<int>(sizeof(float2)) + 128 +
-                             kSpreadWarps * 32 * point_scratch<K>() * static_cast<int>(sizeof(float));
-            auto kernel = k_batch_spread<K>;
-            if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-            B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSpreadWarps * 32, smem));
-            const int chunk = b->plans[0]->chunk;
-            const long long items = static_cast<long long>(b->total_chunks) * ((chunk + kSpreadItem - 1) / kSpreadItem);
-            const int blocks = static_cast<int>(std::max(1LL, std::min<long long>((items + kSpreadWarps - 1) / kSpreadWarps,
-                                                                            std::max(per_sm, 1) * sms)));
-            B_TRY(cudaMemsetAsync(b->d_work, 0, sizeof(int), b->stream));
-            kernel<<<blocks, kSpreadWarps * 32, smem, b->stream>>>(b->d_desc, n, b->d_io, b->total_chunks, g0,
-                                                                   b->poly, chunk, b->d_work, b->d_status);
-            B_TRY(cudaGetLastError());
-        }
+        int st;
+        for (const auto &kg : b->kgroups)
+            if ((st = launch_spread_k(b, kg, sms)) != NFFT2D_OK) return st;
         k_batch_fold<<<dim3(16, n), kThreads, 0, b->stream>>>(b->d_desc);
         B_TRY(cudaGetLastError());
-        int st = run_ffts(b, type == 1 ? CUFFT_INVERSE : CUFFT_FORWARD);
+        st = run_ffts(b, type == 1 ? CUFFT_INVERSE : CUFFT_FORWARD);
         if (st != NFFT2D_OK) return st;
         k_batch_crop<<<b->total_crop, kThreads, 0, b->stream>>>(b->d_desc, n, b->d_io);
         B_TRY(cudaGetLastError());
@@ -389,34 +448,22 @@ int enqueue_stages(nfft2d_batch_s *b, int type) {
     return NFFT2D_OK;
 }
 
-int enqueue(nfft2d_batch_s *b, int type) {
-    switch (b->K) {
-        case 2: return enqueue_stages<2>(b, type);
-        case 3: return enqueue_stages<3>(b, type);
-        case 4: return enqueue_stages<4>(b, type);
-        case 5: return enqueue_stages<5>(b, type);
-        case 6: return enqueue_stages<6>(b, type);
-        case 7: return enqueue_stages<7>(b, type);
-        case 8: return enqueue_stages<8>(b, type);
-        default: return NFFT2D_ERR_INVALID_ARG;
-    }
-}
-
 int run(nfft2d_batch_s *b, int type, const void *const *in, void *const *out) {
     if (!b || !in || !out) return NFFT2D_ERR_INVALID_ARG;
     if (!b->points_valid) return NFFT2D_ERR_NO_POINTS;
     // the point-side array of a transform with no points may be null
-    for (int t = 0; t < b->count; ++t) {
-        const bool empty = b->plans[t]->M == 0;
+    for (int i = 0; i < b->count; ++i) {
+        const int t = b->order[i];
+        const bool empty = b->plans[i]->M == 0;
         const void *coef = type == 2 ? in[t] : out[t];
         const void *pts = type == 2 ? out[t] : in[t];
         if (!coef || (!pts && !empty)) return NFFT2D_ERR_INVALID_ARG;
     }
     // the previous copy of the pointer table must have left the pinned buffer
     if (b->io_pending) B_TRY(cudaEventSynchronize(b->ev_io));
-    for (int t = 0; t < b->count; ++t) {
-        b->h_io[t].in = static_cast<const float2 *>(in[t]);
-        b->h_io[t].out = static_cast<float2 *>(out[t]);
+    for (int i = 0; i < b->count; ++i) {  // the table is in the internal order
+        b->h_io[i].in = static_cast<const float2 *>(in[b->order[i]]);
+        b->h_io[i].out = static_cast<float2 *>(out[b->order[i]]);
     }
     B_TRY(cudaEventRecord(b->ev_in, b->user_stream));
     B_TRY(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
@@ -453,13 +500,13 @@ int run(nfft2d_batch_s *b, int type, const void *const *in, void *const *out) {
 
 extern "C" {
 
-int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *N2, double sigma, int K,
-                        void *stream) {
-    if (!out || count <= 0 || !N1 || !N2) return NFFT2D_ERR_INVALID_ARG;
+int nfft2d_batch_create_k(nfft2d_batch *out, int count, const int *N1, const int *N2, const int *K, double sigma,
+                          void *stream) {
+    if (!out || count <= 0 || !N1 || !N2 || !K) return NFFT2D_ERR_INVALID_ARG;
     *out = nullptr;
     for (int t = 0; t < count; ++t) {
         Geom g{};
-        const int st = compute_layout(N1[t], N2[t], sigma, K, NFFT2D_F32, kRegTile, &g, nullptr, nullptr);
+        const int st = compute_layout(N1[t], N2[t], sigma, K[t], NFFT2D_F32, kRegTile, &g, nullptr, nullptr);
         if (st != NFFT2D_OK) return st;
     }
     nfft2d_batch_s *b = new (std::nothrow) nfft2d_batch_s();
@@ -469,31 +516,38 @@ int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *
         return s;
     };
     b->count = count;
-    b->K = K;
     b->sigma = sigma;
     b->user_stream = static_cast<cudaStream_t>(stream);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     for (auto *e : {&b->ev_in, &b->ev_out, &b->ev_io})
         if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
 
-    // group by size; lay the grids out group by group
-    std::map<std::pair<int, int>, std::vector<int>> by_size;
-    for (int t = 0; t < count; ++t) by_size[{N1[t], N2[t]}].push_back(t);
+    // internal order by (K, N1, N2); the grid pitch depends on K (the patch
+    // padding), so cuFFT size groups are (K, N1, N2) groups, laid out group by
+    // group in one allocation
+    b->order.resize(count);
+    for (int t = 0; t < count; ++t) b->order[t] = t;
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) {
+        return std::make_tuple(K[a], N1[a], N2[a]) < std::make_tuple(K[c], N1[c], N2[c]);
+    });
     std::vector<size_t> offset(count);
     size_t elems = 0;
-    for (auto &kv : by_size) {
-        nfft2d_batch_s::Group gr;
-        gr.N1 = kv.first.first;
-        gr.N2 = kv.first.second;
-        gr.members = kv.second;
-        Geom g{};
-        compute_layout(gr.N1, gr.N2, sigma, K, NFFT2D_F32, kRegTile, &g, nullptr, nullptr);
-        gr.first_elem = elems;
-        for (int t : gr.members) {
-            offset[t] = elems;
-            elems += static_cast<size_t>(g.Ra) * g.C;
+    for (int i = 0; i < count; ++i) {
+        const int t = b->order[i];
+        if (b->groups.empty() || b->groups.back().K != K[t] || b->groups.back().N1 != N1[t] ||
+            b->groups.back().N2 != N2[t]) {
+            nfft2d_batch_s::Group gr;
+            gr.K = K[t];
+            gr.N1 = N1[t];
+            gr.N2 = N2[t];
+            gr.first_elem = elems;
+            b->groups.push_back(gr);
         }
-        b->groups.push_back(gr);
+        b->groups.back().members.push_back(i);
+        Geom g{};
+        compute_layout(N1[t], N2[t], sigma, K[t], NFFT2D_F32, kRegTile, &g, nullptr, nullptr);
+        offset[i] = elems;
+        elems += static_cast<size_t>(g.Ra) * g.C;
     }
     b->grid_bytes = elems * sizeof(float2);
     // 256 zeroed bytes of slack after the last grid: the direct gather may
@@ -501,9 +555,10 @@ int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *
     if (cudaMalloc(&b->grids, b->grid_bytes + 256) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMemsetAsync(b->grids, 0, b->grid_bytes + 256, b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     b->plans.assign(count, nullptr);
-    for (int t = 0; t < count; ++t) {
-        const int st = create_plan(&b->plans[t], N1[t], N2[t], sigma, K, NFFT2D_F32, kRegTile, b->stream,
-                                   static_cast<float2 *>(b->grids) + offset[t]);
+    for (int i = 0; i < count; ++i) {
+        const int t = b->order[i];
+        const int st = create_plan(&b->plans[i], N1[t], N2[t], sigma, K[t], NFFT2D_F32, kRegTile, b->stream,
+                                   static_cast<float2 *>(b->grids) + offset[i]);
         if (st != NFFT2D_OK) return fail(st);
     }
     for (auto &gr : b->groups) {
@@ -516,17 +571,35 @@ int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *
         gr.fft_ok = true;
         if (cufftSetStream(gr.fft, b->stream) != CUFFT_SUCCESS) return fail(NFFT2D_ERR_CUFFT);
     }
+    // window-width groups: contiguous in the internal order
+    for (int i = 0; i < count; ++i) {
+        const int k = b->plans[i]->K;
+        if (b->kgroups.empty() || b->kgroups.back().K != k) {
+            nfft2d_batch_s::KGroup kg;
+            kg.K = k;
+            kg.first = i;
+            kg.g0 = b->plans[i]->g;
+            kg.poly = b->plans[i]->poly;
+            b->kgroups.push_back(kg);
+        }
+        ++b->kgroups.back().n;
+    }
     if (cudaMalloc(&b->d_desc, sizeof(BatchDesc) * count) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMalloc(&b->d_io, sizeof(BatchIO) * count) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMallocHost(&b->h_io, sizeof(BatchIO) * count) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMalloc(&b->d_work, sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMalloc(&b->d_status, 4 * sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     if (cudaMemsetAsync(b->d_status, 0, 4 * sizeof(int), b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
-    b->g0 = b->plans[0]->g;
-    b->poly = b->plans[0]->poly;
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     *out = b;
     return NFFT2D_OK;
+}
+
+int nfft2d_batch_create(nfft2d_batch *out, int count, const int *N1, const int *N2, double sigma, int K,
+                        void *stream) {
+    if (count <= 0) return NFFT2D_ERR_INVALID_ARG;
+    const std::vector<int> Ks(static_cast<size_t>(count), K);
+    return nfft2d_batch_create_k(out, count, N1, N2, Ks.data(), sigma, stream);
 }
 
 int nfft2d_batch_destroy(nfft2d_batch b) {
@@ -544,11 +617,12 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
     std::vector<BatchDesc> h(b->count);
     int chunks = 0, rows = 0, crop = 0;
     long long points = 0;
-    for (int t = 0; t < b->count; ++t) {
-        nfft2d_plan_s *p = b->plans[t];
+    for (int i = 0; i < b->count; ++i) {  // internal order; the arguments are in the caller's
+        const int t = b->order[i];
+        nfft2d_plan_s *p = b->plans[i];
         const int st = nfft2d_set_points(p, M[t], x1[t], x2[t], coord_dtype, units);
         if (st != NFFT2D_OK) return st;
-        BatchDesc &D = h[t];
+        BatchDesc &D = h[i];
         std::memset(&D, 0, sizeof(D));
         std::memcpy(&D.tmap, &p->tmap, sizeof(CUtensorMap));
         D.recs = static_cast<const Rec32 *>(p->recs);
@@ -572,6 +646,13 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
     }
     B_TRY(cudaMemcpy(b->d_desc, h.data(), sizeof(BatchDesc) * b->count, cudaMemcpyHostToDevice));
     if (points > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;  // global point indices are int
+    for (auto &kg : b->kgroups) {
+        kg.chunk0 = h[kg.first].chunk_base;
+        kg.point0 = h[kg.first].point_base;
+        const int last = kg.first + kg.n - 1;
+        kg.total_chunks = h[last].chunk_base + h[last].n_chunks - kg.chunk0;
+        kg.total_points = static_cast<int>(h[last].point_base + b->plans[last]->M - kg.point0);
+    }
     b->total_chunks = chunks;
     b->total_points = static_cast<int>(points);
     b->total_rows = rows;

@@ -200,9 +200,11 @@ class Plan:
 class Batch:
     """Many FP32 transforms of uneven size run together (nfft2d_batch_*):
     one batched cuFFT call per size group, one launch per stage for all
-    transforms, the whole stage sequence replayed as a CUDA graph."""
+    transforms (the gather and spread once per window width), the whole
+    stage sequence replayed as a CUDA graph.  K is one window half-width for
+    all transforms or a sequence with one per transform."""
 
-    def __init__(self, sizes, sigma: float = 2.0, K: int = 6, stream: torch.cuda.Stream | None = None,
+    def __init__(self, sizes, sigma: float = 2.0, K=6, stream: torch.cuda.Stream | None = None,
                  graph: bool = True):
         self._lib = _lib.load()
         self.sizes = [(int(a), int(b)) for a, b in sizes]
@@ -211,8 +213,15 @@ class Batch:
         n1 = (ctypes.c_int * self.count)(*[a for a, _ in self.sizes])
         n2 = (ctypes.c_int * self.count)(*[b for _, b in self.sizes])
         h = ctypes.c_void_p()
-        check(self._lib.nfft2d_batch_create(ctypes.byref(h), self.count, n1, n2, float(sigma), int(K),
-                                            ctypes.c_void_p(self.stream.cuda_stream)), "nfft2d_batch_create")
+        if isinstance(K, int):
+            check(self._lib.nfft2d_batch_create(ctypes.byref(h), self.count, n1, n2, float(sigma), int(K),
+                                                ctypes.c_void_p(self.stream.cuda_stream)), "nfft2d_batch_create")
+        else:
+            if len(K) != self.count:
+                raise ValueError("K must be an int or hold one value per transform")
+            ks = (ctypes.c_int * self.count)(*[int(k) for k in K])
+            check(self._lib.nfft2d_batch_create_k(ctypes.byref(h), self.count, n1, n2, ks, float(sigma),
+                                                  ctypes.c_void_p(self.stream.cuda_stream)), "nfft2d_batch_create_k")
         self._h = h
         self.M = [0] * self.count
         self._keep = ()

@@ -19,9 +19,9 @@ def _problem(sizes, Ms, seed):
     return xs, Fs, fs
 
 
-def _single(n1, n2, x, F, f):
+def _single(n1, n2, x, F, f, K=6):
     from miscellaneous_gb300.nfft import Plan
-    with Plan(n1, n2) as p:
+    with Plan(n1, n2, K=K) as p:
         p.set_points(torch.from_numpy(x[0]).cuda(), torch.from_numpy(x[1]).cuda())
         a = p.forward(torch.from_numpy(F).cuda().reshape(-1))
         b = p.adjoint(torch.from_numpy(f).cuda())
@@ -99,3 +99,31 @@ def test_pso_shaped_batch_matches_single_plans():
         oR = outs_R[t].cpu().numpy().reshape(-1)
         assert np.linalg.norm(oR - r) / np.linalg.norm(r) < 1e-6
     b.close()
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_uneven_window_widths_in_one_batch(orc, graph):
+    """A K per transform (nfft2d_batch_create_k): transforms in an order that
+    interleaves the widths, including an empty one; each matches its own
+    single plan of the same K, and the exact NDFT at the FP32 bar."""
+    from miscellaneous_gb300.nfft import Batch
+    sizes = [(64, 64), (32, 48), (64, 64), (16, 16), (128, 64), (32, 48), (48, 32), (64, 32)]
+    Ks = [6, 3, 8, 4, 2, 6, 5, 7]
+    Ms = [3000, 700, 2500, 0, 6000, 257, 900, 1500]
+    xs, Fs, fs = _problem(sizes, Ms, 31)
+    with Batch(sizes, K=Ks, graph=graph) as bt:
+        bt.set_points([torch.from_numpy(x[0]).cuda() for x in xs], [torch.from_numpy(x[1]).cuda() for x in xs])
+        outs = bt.forward([torch.from_numpy(F).cuda().reshape(-1) for F in Fs])
+        adjs = bt.adjoint([torch.from_numpy(f).cuda() for f in fs])
+        bt.synchronize()
+        for t, ((n1, n2), K, x, F, f) in enumerate(zip(sizes, Ks, xs, Fs, fs)):
+            got_f, got_F = outs[t].cpu().numpy(), adjs[t].cpu().numpy()
+            if Ms[t] == 0:
+                assert got_f.size == 0 and np.all(got_F == 0)
+                continue
+            a, b = _single(n1, n2, x, F, f, K=K)
+            assert orc.rel_l2(got_f, a) < 1e-6, t
+            assert orc.rel_l2(got_F, b) < 1e-6, t
+            g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
+            bar = 1e-5 if K >= 3 else 1e-3  # the window itself is off by 4e-4 at K = 2 (sigma = 2)
+            assert orc.rel_l2(got_f, orc.ndft_type2(F, g1, g2, sign=-1)) < bar, t

@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kThreads)
         latch_error(status, kErrBounds);
         return;
     }
-    io[t].out[raw.w] = gather_direct_f32<K>(D.grid, __ldg(&D.g.H), __ldg(&D.g.C), mu1, mu2, __int_as_float(raw.x),
+    io[t].out[raw.w] = gather_direct_f32<K, true>(D.grid, __ldg(&D.g.H), __ldg(&D.g.C), mu1, mu2, __int_as_float(raw.x),
                                             __int_as_float(raw.y), wp);
 }
 

@@ -194,7 +194,8 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
     weights_any<K, Real>(static_cast<Real>(r.t1), w1, a);
     weights_any<K, Real>(static_cast<Real>(r.t2), w2, a);
     if constexpr (MODE == 0 && sizeof(Real) == 4) {
-        out[r.orig] = gather_direct_f32<K>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
+        out[r.orig] = a.compensated ? gather_direct_f32<K, true>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly)
+                                    : gather_direct_f32<K, false>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
     } else if (MODE == 0) {
         Real sx = 0, sy = 0;
 #pragma unroll

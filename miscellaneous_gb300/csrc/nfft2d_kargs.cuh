@@ -15,6 +15,7 @@ struct KArgs {
     int n_chunks;            // work items (tiled kernels)
     int M;                   // points (direct kernels)
     int chunk;               // maximum points per work item of the chunk list
+    int compensated;         // FP32 gathers: compensated (TwoSum) sum over the rows
     int *status;             // [1]: latched error bits
     WinPoly poly;            // FP32 window polynomials (kernel parameter space)
 };
@@ -33,6 +34,7 @@ inline KArgs make_kargs(const nfft2d_plan_s *p) {
     a.ds2_d = p->xscale2;
     a.n_chunks = static_cast<int>(p->n_chunks);
     a.M = static_cast<int>(p->M);
+    a.compensated = p->compensated;
     a.chunk = p->chunk;
     a.status = p->d_status;
     a.poly = p->poly;

@@ -61,7 +61,11 @@ __device__ __forceinline__ float2 gather_point(const float2 *__restrict__ patch,
 // are read and the column weights shifted by one for odd starts (the extra
 // column gets weight 0; it lies inside the padded grid, or in the zeroed
 // slack after it).  Grid rows start on 16-byte boundaries (even pitch).
-template <int K>
+//
+// COMP: the weighted row partials are summed with TwoSum and the rounding
+// errors carried in a second accumulator (as the tiled gather does), else
+// with plain FMAs.
+template <int K, bool COMP>
 __device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ grid, int H, int C, int mu1, int mu2,
                                                     float t1, float t2, const WinPoly &wp) {
     constexpr int W = 2 * K + 1;
@@ -85,7 +89,7 @@ __device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ g
     float2 wsp[2 * V];
 #pragma unroll
     for (int q = 0; q < 2 * V; ++q) wsp[q] = make_float2(ws[q], ws[q]);
-    float2 s = make_float2(0.f, 0.f);
+    float2 s = make_float2(0.f, 0.f), e = make_float2(0.f, 0.f);
 #pragma unroll
     for (int rr = 0; rr < W; ++rr) {
         const float4 *row = rb + rr * pitch4;
@@ -96,8 +100,17 @@ __device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ g
             r = __ffma2_rn(make_float2(v.x, v.y), wsp[2 * q], r);
             r = __ffma2_rn(make_float2(v.z, v.w), wsp[2 * q + 1], r);
         }
-        s = __ffma2_rn(r, make_float2(w1[rr], w1[rr]), s);
+        if constexpr (COMP) {
+            float ex, ey;
+            two_sum(s.x, __fmul_rn(w1[rr], r.x), s.x, ex);
+            two_sum(s.y, __fmul_rn(w1[rr], r.y), s.y, ey);
+            e.x = __fadd_rn(e.x, ex);
+            e.y = __fadd_rn(e.y, ey);
+        } else {
+            s = __ffma2_rn(r, make_float2(w1[rr], w1[rr]), s);
+        }
     }
+    if constexpr (COMP) return make_float2(s.x + e.x, s.y + e.y);
     return s;
 }
 

@@ -199,7 +199,7 @@ __global__ void k_batch_fold(const BatchDesc *__restrict__ d) {
 // One launch per window width: transforms [first, first + n) of the batch's
 // internal order share K and hold global points [point0, point0 + npoints).
 template <int K>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, K <= 6 ? 4 : 3)  // as the single-plan FP32 gather
     k_batch_gather_direct(const BatchDesc *__restrict__ d, int first, int n, const BatchIO *__restrict__ io,
                           int point0, int npoints, const __grid_constant__ WinPoly wp, int *status) {
     const int i = point0 + blockIdx.x * kThreads + threadIdx.x;

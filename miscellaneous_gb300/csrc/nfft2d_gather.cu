@@ -248,6 +248,28 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
     }
 }
 
+// The FP32 forward gather on its own: bounded to 64 registers (K <= 6) or
+// 80 (K = 7, 8) so that four or three CTAs share an SM.  Its L1 loads are
+// latency-bound, and the compiler's own choice (54 registers at K = 6, with
+// fewer loads in flight) measured 9 % slower on GB300 (polar 65.5 -> 59.4 us,
+// uniform 67.5 -> 61.3 us at K = 6).
+template <int K>
+__global__ void __launch_bounds__(kThreads, K <= 6 ? 4 : 3)
+    k_gather_direct_f32(const float2 *__restrict__ grid, const Rec32 *__restrict__ recs, float2 *__restrict__ out,
+                        const __grid_constant__ KArgs a) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.M) return;
+    const Rec32 r = recs[i];
+    const int mu1 = static_cast<int>(static_cast<unsigned>(r.mu) >> 16), mu2 = r.mu & 0xFFFF;
+    const Geom g = a.g;
+    if (mu1 >= g.n1 || mu2 >= g.n2) {
+        latch_error(a.status, kErrBounds);
+        return;
+    }
+    out[r.orig] = a.compensated ? gather_direct_f32<K, true>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly)
+                                : gather_direct_f32<K, false>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
+}
+
 template <typename KernelT>
 cudaError_t prepare_smem(KernelT kernel, int smem) {
     if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -278,6 +300,9 @@ cudaError_t launch_K(const nfft2d_plan_s *p, void *f, const void *v, void *g1, v
         k_gather_direct<K, double, Rec64, MODE><<<blocks, kThreads, 0, p->stream>>>(
             static_cast<const double2 *>(p->grid), static_cast<const Rec64 *>(p->recs), static_cast<double2 *>(f),
             static_cast<const double2 *>(v), static_cast<double *>(g1), static_cast<double *>(g2), a);
+    } else if constexpr (MODE == 0) {
+        k_gather_direct_f32<K><<<blocks, kThreads, 0, p->stream>>>(
+            static_cast<const float2 *>(p->grid), static_cast<const Rec32 *>(p->recs), static_cast<float2 *>(f), a);
     } else {
         k_gather_direct<K, float, Rec32, MODE><<<blocks, kThreads, 0, p->stream>>>(
             static_cast<const float2 *>(p->grid), static_cast<const Rec32 *>(p->recs), static_cast<float2 *>(f),

@@ -15,8 +15,10 @@
 // (TwoSum) when enabled.
 //
 // DIRECT variant (both precisions): one thread per sorted point reads its
-// taps straight from the padded grid (L1/L2), no shared memory; FP32 reads
-// two taps per 16-byte load.
+// taps straight from the padded grid (L1/L2), no shared memory.  FP32 plans
+// use k_gather_direct_f32 / k_grad_direct_f32 (two taps per 16-byte load,
+// bounded registers, compensated row sum in the gather); FP64 plans the
+// generic k_gather_direct.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -193,10 +195,7 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
     Real w1[W], w2[W];
     weights_any<K, Real>(static_cast<Real>(r.t1), w1, a);
     weights_any<K, Real>(static_cast<Real>(r.t2), w2, a);
-    if constexpr (MODE == 0 && sizeof(Real) == 4) {
-        out[r.orig] = a.compensated ? gather_direct_f32<K, true>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly)
-                                    : gather_direct_f32<K, false>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
-    } else if (MODE == 0) {
+    if constexpr (MODE == 0) {
         Real sx = 0, sy = 0;
 #pragma unroll
         for (int rr = 0; rr < W; ++rr) {
@@ -270,6 +269,67 @@ __global__ void __launch_bounds__(kThreads, K <= 6 ? 4 : 3)
                                 : gather_direct_f32<K, false>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
 }
 
+// The FP32 coordinate gradient with the forward gather's 16-byte row loads:
+// per row the value and slope column weights (shifted by one for odd starts,
+// as in gather_direct_f32) give the partials r = sum w2 v and q = sum dw2 v;
+// then d f/d t1 = sum dw1 r and d f/d t2 = sum w1 q.
+template <int K>
+__global__ void __launch_bounds__(kThreads, K <= 6 ? 3 : 2)
+    k_grad_direct_f32(const float2 *__restrict__ grid, const Rec32 *__restrict__ recs,
+                      const float2 *__restrict__ vin, float *__restrict__ g1, float *__restrict__ g2,
+                      const __grid_constant__ KArgs a) {
+    constexpr int W = 2 * K + 1;
+    constexpr int V = K + 1;  // float4 loads per row
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.M) return;
+    const Rec32 r = recs[i];
+    const int mu1 = static_cast<int>(static_cast<unsigned>(r.mu) >> 16), mu2 = r.mu & 0xFFFF;
+    const Geom g = a.g;
+    if (mu1 >= g.n1 || mu2 >= g.n2) {
+        latch_error(a.status, kErrBounds);
+        return;
+    }
+    float w1[W], d1[W], w2[W], d2[W];
+    weights_poly_d<K>(r.t1, w1, d1, a.poly);
+    weights_poly_d<K>(r.t2, w2, d2, a.poly);
+    const int col0 = mu2 + g.H - K;
+    const int odd = col0 & 1;
+    float ws[2 * V], ds[2 * V];
+#pragma unroll
+    for (int q = 0; q < 2 * V; ++q) {
+        const bool lo_in = q < W, hi_in = q >= 1 && q - 1 < W;
+        ws[q] = odd ? (hi_in ? w2[q - 1] : 0.f) : (lo_in ? w2[q] : 0.f);
+        ds[q] = odd ? (hi_in ? d2[q - 1] : 0.f) : (lo_in ? d2[q] : 0.f);
+    }
+    const float4 *rb = reinterpret_cast<const float4 *>(grid + static_cast<size_t>(mu1 + g.H - K) * g.C + (col0 - odd));
+    const int pitch4 = g.C >> 1;
+    float ax = 0.f, ay = 0.f, bx = 0.f, by = 0.f;
+#pragma unroll
+    for (int rr = 0; rr < W; ++rr) {
+        const float4 *row = rb + rr * pitch4;
+        float rx = 0.f, ry = 0.f, qx = 0.f, qy = 0.f;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            const float4 v = __ldg(row + q);
+            rx = fmaf(ws[2 * q], v.x, rx);
+            ry = fmaf(ws[2 * q], v.y, ry);
+            qx = fmaf(ds[2 * q], v.x, qx);
+            qy = fmaf(ds[2 * q], v.y, qy);
+            rx = fmaf(ws[2 * q + 1], v.z, rx);
+            ry = fmaf(ws[2 * q + 1], v.w, ry);
+            qx = fmaf(ds[2 * q + 1], v.z, qx);
+            qy = fmaf(ds[2 * q + 1], v.w, qy);
+        }
+        ax = fmaf(d1[rr], rx, ax);
+        ay = fmaf(d1[rr], ry, ay);
+        bx = fmaf(w1[rr], qx, bx);
+        by = fmaf(w1[rr], qy, by);
+    }
+    const float2 v = __ldg(&vin[r.orig]);
+    g1[r.orig] = a.ds1 * (v.x * ax + v.y * ay);
+    g2[r.orig] = a.ds2 * (v.x * bx + v.y * by);
+}
+
 template <typename KernelT>
 cudaError_t prepare_smem(KernelT kernel, int smem) {
     if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -304,9 +364,10 @@ cudaError_t launch_K(const nfft2d_plan_s *p, void *f, const void *v, void *g1, v
         k_gather_direct_f32<K><<<blocks, kThreads, 0, p->stream>>>(
             static_cast<const float2 *>(p->grid), static_cast<const Rec32 *>(p->recs), static_cast<float2 *>(f), a);
     } else {
-        k_gather_direct<K, float, Rec32, MODE><<<blocks, kThreads, 0, p->stream>>>(
-            static_cast<const float2 *>(p->grid), static_cast<const Rec32 *>(p->recs), static_cast<float2 *>(f),
-            static_cast<const float2 *>(v), static_cast<float *>(g1), static_cast<float *>(g2), a);
+        static_assert(MODE == 0 || MODE == 1, "gather (0) or coordinate gradient (1)");
+        k_grad_direct_f32<K><<<blocks, kThreads, 0, p->stream>>>(
+            static_cast<const float2 *>(p->grid), static_cast<const Rec32 *>(p->recs), static_cast<const float2 *>(v),
+            static_cast<float *>(g1), static_cast<float *>(g2), a);
     }
     return cudaGetLastError();
 }

@@ -11,11 +11,20 @@ sign +1) over the same points with the points already binned (the plan is
 reused, as a solver iteration does).  value = points per second through one
 forward+adjoint pair = M / step time.  The working set (about 50 MB) fits in
 L2, so a 256 MB buffer is written between timed steps (outside the timed
-events) to flush it.
+events) to flush it.  The timed steps run without the plan's per-stage
+events; the stage breakdown (stages_ms, and the roofline's kernel time)
+comes from as many further steps with them.
 
 e2e = the same metric through the public API with HOST (pinned) buffers:
 each step copies x1, x2, F and f host->device, bins the points
-(set_points), runs forward + adjoint and copies f_out and F_out back.
+(set_points, asynchronous), runs forward + adjoint and copies f_out and
+F_out back; L2 is flushed between these steps too.
+
+Other workloads (--workload): config1 (64^2, 4096 points), clustered (2048^2,
+2^24 points, --K 4/6/8), batch (64 uneven transforms), pso (250 transforms
+on 44^2), lsq (least-squares gradient step, 1024^2, 2^22 points), knab (the
+Knab-window regridding of a 1024^2 raster onto 2048^2 outputs).  Every line
+reports rel-L2 against FP64 sums on a subset of the points.
 
 --impl reference times the reference's CPU algorithm (the C restatement of
 NFFT1_2D.m / NFFT2_2D.m in oracle/, OpenMP over all host cores) on the same

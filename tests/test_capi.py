@@ -120,6 +120,30 @@ def test_null_plan_is_rejected(lib):
     assert lib.nfft2d_ndft2d_f64(None, None, None, None, None, None, 8, 8, 0, 0, -1, None) == 0
 
 
+def test_batch_create_validates_before_touching_the_device(lib):
+    h = ctypes.c_void_p()
+    n1 = (ctypes.c_int * 3)(64, 32, 48)
+    n2 = (ctypes.c_int * 3)(64, 32, 48)
+    for ks in ((6, 1, 6), (6, 9, 6)):  # a half-width outside 2..8
+        k = (ctypes.c_int * 3)(*ks)
+        assert lib.nfft2d_batch_create_k(ctypes.byref(h), 3, n1, n2, k, 2.0, None) == _lib.ERR_INVALID_ARG
+    k = (ctypes.c_int * 3)(6, 3, 8)
+    assert lib.nfft2d_batch_create_k(ctypes.byref(h), 0, n1, n2, k, 2.0, None) == _lib.ERR_INVALID_ARG
+    assert lib.nfft2d_batch_create_k(ctypes.byref(h), 3, n1, n2, None, 2.0, None) == _lib.ERR_INVALID_ARG
+    odd = (ctypes.c_int * 3)(64, 33, 48)
+    assert lib.nfft2d_batch_create_k(ctypes.byref(h), 3, odd, n2, k, 2.0, None) == _lib.ERR_INVALID_ARG
+    assert lib.nfft2d_batch_create(ctypes.byref(h), 3, odd, n2, 2.0, 6, None) == _lib.ERR_INVALID_ARG
+    assert not h.value
+    assert lib.nfft2d_set_points_async(None, 0, None, None, 0, 0) == _lib.ERR_INVALID_ARG
+
+
+def test_python_batch_rejects_mismatched_widths():
+    import pytest as _pt
+    from miscellaneous_gb300.nfft import Batch
+    with _pt.raises(ValueError):
+        Batch([(64, 64), (32, 32)], K=[6, 4, 8], stream=object())
+
+
 def test_no_gpu_plan_create_reports_cuda_error(lib):
     try:
         import torch

@@ -1,6 +1,9 @@
 // nfft2d_plan.cu -- plan life cycle, point binning (counting sort by tile and
-// cell), the small grid kernels (deapodize+pad, halo fill/fold, crop+deapodize)
-// and the C ABI entry points of libnfft2d_gb300.so.
+// cell with single-pass look-back scans), the small grid kernels (deapodize+
+// pad, halo fill/fold, crop+deapodize: used around cuFFT) and the C ABI entry
+// points of libnfft2d_gb300.so.  The oversampled FFT is the fused passes of
+// nfft2d_fft.cu for FP32 plans on power-of-two grids below 2048 x 2048 cells
+// (use_fused), cuFFT otherwise (run_fft).
 //
 // Reference path being replaced: NFFT/NFFT2_2D.cu:329-495 (NFFT2_2D_GPU:
 // constants, Kernel_Bessel, malloc/memset, Interpolation_NFFT2_2D_GPUKernel,

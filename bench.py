@@ -1,34 +1,39 @@
 """Benchmark of the 2D NFFT hot path on GB300.
 
-Workload (default): the polar-raster NFFT, SAR back-projection shape --
-N = 512 x 512 complex64 coefficients (re/im ~ N(0,1)), 512 spokes x 2048
-radial samples = 1,048,576 points on diametral lines of radius 0.5 with
-uniform jitter +-1e-3 per coordinate, wrapped into [-0.5, 0.5)^2; sigma = 2,
-w = K = 6 (13 x 13 taps), FP32.  Seeded synthetic data (PCG64, seed 1).
+Workload (default): the large clustered NFFT, the largest single-GPU
+configuration -- N = 2048 x 2048 complex64 coefficients (re/im ~ N(0,1)),
+M = 2^24 points with each coordinate ~ N(0, 0.15^2) wrapped into
+[-0.5, 0.5); sigma = 2, w = K = 6 (13 x 13 taps), FP32 with compensated
+gather accumulation and FP64 coordinate reduction and deapodization tables.
+Seeded synthetic data (NumPy PCG64, seed 3).  The configuration is a
+precision study: the line also carries the step time and the error of
+w = 4 and w = 8 on the same points (precision_study).
 
 One step = one forward (type 2, reference NFFT1_2D) + one adjoint (type 1,
 sign +1) over the same points with the points already binned (the plan is
 reused, as a solver iteration does).  value = points per second through one
-forward+adjoint pair = M / step time.  The working set (about 50 MB) fits in
-L2, so a 256 MB buffer is written between timed steps (outside the timed
-events) to flush it.  The timed steps run without the plan's per-stage
-events; the stage breakdown (stages_ms, and the roofline's kernel time)
-comes from as many further steps with them.
+forward+adjoint pair = M / step time.  The working set (about 700 MB) is
+larger than L2, and a 256 MB buffer is written between timed steps (outside
+the timed events) all the same.  The timed steps run without the plan's
+per-stage events; the stage breakdown (stages_ms, and the roofline's kernel
+time) comes from as many further steps with them.
 
 e2e = the same metric through the public API with HOST (pinned) buffers:
 each step copies x1, x2, F and f host->device, bins the points
 (set_points, asynchronous), runs forward + adjoint and copies f_out and
 F_out back; L2 is flushed between these steps too.
 
-Other workloads (--workload): config1 (64^2, 4096 points), clustered (2048^2,
-2^24 points, --K 4/6/8), batch (64 uneven transforms), pso (250 transforms
-on 44^2), lsq (least-squares gradient step, 1024^2, 2^22 points), knab (the
-Knab-window regridding of a 1024^2 raster onto 2048^2 outputs).  Every line
-reports rel-L2 against FP64 sums on a subset of the points.
+Other workloads (--workload): polar (the SAR polar raster, 512^2, 2^20
+points), config1 (64^2, 4096 points), batch (64 uneven transforms), pso (250
+transforms on 44^2), lsq (least-squares gradient step, 1024^2, 2^22 points),
+knab (the Knab-window regridding of a 1024^2 raster onto 2048^2 outputs).
+Every line reports rel-L2 against FP64 sums on a subset of the points.
 
 --impl reference times the reference's CPU algorithm (the C restatement of
 NFFT1_2D.m / NFFT2_2D.m in oracle/, OpenMP over all host cores) on the same
-workload.
+workload, and the reference's own GPU spreading (NFFT/NFFT2_2D.cu, built
+into oracle/_ref) on two small shapes (reference_gpu_spread); the library's
+line carries its own times on those shapes (spread_small_cases).
 """
 from __future__ import annotations
 
@@ -58,7 +63,7 @@ L2_FLUSH_BYTES = 256 << 20
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-def polar_raster(seed: int = 1, spokes: int = 512, samples: int = 2048, N: int = 512, jitter: float = 1e-3):
+def polar_raster(seed: int = 2, spokes: int = 512, samples: int = 2048, N: int = 512, jitter: float = 1e-3):
     rng = np.random.default_rng(seed)
     theta = np.pi * np.arange(spokes) / spokes
     r = -0.5 + np.arange(samples) / samples
@@ -88,7 +93,7 @@ def uniform_config1(seed: int = 0):
                         "w": 6, "seed": seed})
 
 
-def clustered_config3(seed: int = 2, K: int = 6, M: int = 1 << 24, N: int = 2048):
+def clustered_config3(seed: int = 3, K: int = 6, M: int = 1 << 24, N: int = 2048):
     rng = np.random.default_rng(seed)
     x1 = np.mod(rng.normal(0.0, 0.15, M) + 0.5, 1.0) - 0.5
     x2 = np.mod(rng.normal(0.0, 0.15, M) + 0.5, 1.0) - 0.5
@@ -100,7 +105,7 @@ def clustered_config3(seed: int = 2, K: int = 6, M: int = 1 << 24, N: int = 2048
                         "seed": seed})
 
 
-def least_squares_config5(seed: int = 4, N: int = 1024, M: int = 1 << 22, noise: float = 1e-3):
+def least_squares_config5(seed: int = 5, N: int = 1024, M: int = 1 << 22, noise: float = 1e-3):
     """L(f, x) = ||NFFT(f; x) - y||^2 with y = NFFT(f_true; x) + CN(0, noise^2):
     N = 1024^2, M = 2^22 uniform points, sigma 2, w 6 (y is built on the GPU)."""
     rng = np.random.default_rng(seed)
@@ -139,7 +144,7 @@ def knab_regrid(seed: int = 5, N: int = 1024, L: int = 2048):
                         "P": 18, "sigma": 2.0, "w": 6, "bandwidth": "0.5/T", "seed": seed})
 
 
-def uneven_batch(seed: int = 3, count: int = 64):
+def uneven_batch(seed: int = 4, count: int = 64):
     """64 transforms, N = 2^e with e ~ U{7..10} (square), M log-uniform in
     [1e4, 4e6], points uniform, coefficients N(0,1) complex; sigma 2, w 6."""
     rng = np.random.default_rng(seed)
@@ -394,11 +399,13 @@ def cpu_baseline(wl, target_s: float = 15.0, steps: int | None = None):
         b = max((t - t2) / (m - m2), 0.0)
         a = max(t - b * m, 0.0)
         out["value"] = M / (a + b * M)
+        out["extrapolated"] = True
         out["model"] = {"grid_s": a, "per_point_s": b, "small_sample_points": m2, "small_sample_ms": t2 * 1e3}
         how = (f"{m} and {m2} of {M} points (random subsets) with the full {wl['N1']}x{wl['N2']} grid; value is "
                f"M / (a + b M) from the two medians")
     else:
         out["value"] = m / t
+        out["extrapolated"] = False
         how = f"all {M} points with the full {wl['N1']}x{wl['N2']} grid"
     out["sample"] = (f"{how}; forward+adjoint per step, median of {n} steps, oracle/nfft2d_oracle.c "
                      f"(restated NFFT1_2D.m + NFFT2_2D.m, OpenMP)")
@@ -408,6 +415,92 @@ def cpu_baseline(wl, target_s: float = 15.0, steps: int | None = None):
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
+def small_spread_cases():
+    """The two shapes on which the reference's own GPU spreading
+    (NFFT/NFFT2_2D.cu, NFFT2_2D_GPU: one child grid of 13 x 13 threads per
+    point) is timed beside the library's: config 1 (64 x 64, 4096 uniform
+    points, PCG64 seed 0) and a 65,536-point random subset of the polar
+    raster (512 x 512).  Coordinates in grid units, complex64 values."""
+    cases = []
+    rng = np.random.default_rng(0)
+    x = (rng.uniform(-0.5, 0.5, 4096) * 64).astype(np.float32)
+    y = (rng.uniform(-0.5, 0.5, 4096) * 64).astype(np.float32)
+    d = (rng.uniform(-1, 1, 4096) + 1j * rng.uniform(-1, 1, 4096)).astype(np.complex64)
+    cases.append(("uniform_64x64_4096", 64, 64, x, y, d))
+    wl = polar_raster()
+    idx = np.sort(np.random.default_rng(65536).choice(wl["x1"].size, 65536, replace=False))
+    cases.append(("polar_raster_512x512_subset_65536", 512, 512, (wl["x1"][idx] * 512).astype(np.float32),
+                  (wl["x2"][idx] * 512).astype(np.float32), wl["f"][idx]))
+    return cases
+
+
+def reference_gpu_spread(reps: int = 5):
+    """Time the reference's own GPU spreading (oracle/_ref: NFFT2_2D.cu
+    compiled unchanged, host side restated) on small_spread_cases():
+    the interpolation kernel with its child grids (CUDA events) and the whole
+    NFFT2_2D_GPU call (host clock: per-call constants, allocations and
+    synchronisations included).  Medians of `reps` calls after one warm-up."""
+    try:
+        import torch
+
+        from oracle import ref_gpu
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device"}
+        if not ref_gpu.available():
+            return {"unavailable": "oracle/_ref/nfft2_2d_ref.cubin was not built"}
+        out = {}
+        for name, N1, N2, x, y, d in small_spread_cases():
+            dev = torch.device("cuda", 0)
+            tx, ty, td = (torch.from_numpy(a).to(dev) for a in (x, y, d))
+            ref_gpu.nfft2_2d_gpu(td, tx, ty, N1, N2)
+            ti, tt = [], []
+            for _ in range(reps):
+                _, a, b = ref_gpu.nfft2_2d_gpu(td, tx, ty, N1, N2, timing=True)
+                ti.append(a)
+                tt.append(b)
+            out[name] = {"interpolation_kernel_ms": statistics.median(ti), "call_ms": statistics.median(tt),
+                         "points": int(x.size)}
+        out["note"] = ("reference NFFT2_2D_GPU float overload (sigma 2, K 6) on the GPU: interpolation = "
+                       "Interpolation_NFFT2_2D_GPUKernel with its per-point series_terms child grids (CUDA events); "
+                       "call = the whole call by host clock")
+        return out
+    except Exception as e:  # the CPU line must still print
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def spread_small_cases(stream, reps: int = 5):
+    """The library's type-1 spreading with the reference's sign on
+    small_spread_cases(): the spread kernel (plan events, grid zeroing
+    included) and the whole type-1 call (CUDA events on the plan's stream)."""
+    import torch
+
+    from miscellaneous_gb300.nfft import Plan
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, N1, N2, x, y, d in small_spread_cases():
+        tx, ty, td = (torch.from_numpy(a).to(dev) for a in (x, y, d))
+        F = torch.empty(N1 * N2, dtype=torch.complex64, device=dev)
+        with Plan(N1, N2, sigma=2.0, K=6, precision="f32", stream=stream) as p:
+            p.set_points(tx, ty, units="grid")
+            p.spread_ref(td, out=F)
+            p.enable_timing(True)
+            ks, cs = [], []
+            for _ in range(reps):
+                ev0.record(stream)
+                p.spread_ref(td, out=F)
+                ev1.record(stream)
+                ev1.synchronize()
+                cs.append(ev0.elapsed_time(ev1))
+                ks.append(p.timings()["spread_ms"])
+            p.synchronize()
+        out[name] = {"spread_kernel_ms": statistics.median(ks), "call_ms": statistics.median(cs),
+                     "points": int(x.size)}
+    out["note"] = ("nfft2d_spread_ref (type 1, sign -1, sigma 2, K 6) on the shapes the reference arm times the "
+                   "reference's own GPU spreading on; spread = grid zeroing + spread kernel (plan events)")
+    return out
+
+
 def run_reference(args, wl):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -422,17 +515,77 @@ def run_reference(args, wl):
         cpu_reference_step(wl, idx)
     times = [cpu_reference_step(wl, idx) for _ in range(args.steps)]
     t = sum(times) / len(times)
-    value = m / t
-    cb = {"value": value, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
-          "sample": (f"{m} of {M} points with the full {wl['N1']}x{wl['N2']} grid per step; "
-                     "oracle/nfft2d_oracle.c restates NFFT1_2D.m (forward) and NFFT2_2D.m (spreading, sign +1); "
-                     "the reference's MATLAB and CUDA code cannot run on the host")}
+    cb = {"unit": UNIT, "cores": oracle.get_threads(), "kind": "port"}
+    if m < M:
+        # t(m) = a + b m from a second, 4x smaller sample: the rate for all M points
+        m2 = max(1, m // 4)
+        idx2 = _cpu_sample(wl, np.random.default_rng(321), m2)
+        t2 = statistics.median([cpu_reference_step(wl, idx2) for _ in range(3)])
+        b = max((t - t2) / (m - m2), 0.0)
+        a = max(t - b * m, 0.0)
+        value = M / (a + b * M)
+        cb.update(extrapolated=True, model={"grid_s": a, "per_point_s": b, "sample_points": m,
+                                            "small_sample_points": m2, "small_sample_ms": t2 * 1e3})
+        how = (f"{m} of {M} points with the full {wl['N1']}x{wl['N2']} grid per step (and {m2} points for the "
+               f"model t(m) = a + b m); value = M / (a + b M)")
+    else:
+        value = m / t
+        cb.update(extrapolated=False)
+        how = f"all {M} points with the full {wl['N1']}x{wl['N2']} grid per step"
+    cb.update(value=value, sample=(f"{how}; oracle/nfft2d_oracle.c restates NFFT1_2D.m (forward) and NFFT2_2D.m "
+                                   "(spreading, sign +1), OpenMP over the host cores; the reference's MATLAB code "
+                                   "cannot run on the host"))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": wl["config"], "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_reference_gpu:
+        line["reference_gpu_spread"] = reference_gpu_spread()
     print(json.dumps(line))
+
+
+def precision_study(args, wl, widths, x1, x2, F, f, stream, flush, torch):
+    """The clustered configuration is a precision study across the window
+    half-width: for each further w, a plan on the same resident points, the
+    same timed forward + adjoint step (CUDA events, L2 flushed between
+    steps) and the same subset accuracy."""
+    from miscellaneous_gb300.nfft import Plan
+    N1, N2, M = wl["N1"], wl["N2"], x1.numel()
+    out = {}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    f_out = torch.empty(M, dtype=torch.complex64, device=x1.device)
+    F_out = torch.empty(N1 * N2, dtype=torch.complex64, device=x1.device)
+    for K in widths:
+        p = Plan(N1, N2, sigma=wl["sigma"], K=K, precision="f32", stream=stream)
+        p.set_points(x1, x2, units="unit")
+        for _ in range(args.warmup):
+            p.forward(F, out=f_out)
+            p.adjoint(f, out=F_out)
+            flush.zero_()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            ev0.record(stream)
+            p.forward(F, out=f_out)
+            p.adjoint(f, out=F_out)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+            flush.zero_()
+        p.synchronize()
+        t = sum(ms) / len(ms)
+        entry = {"ms_per_step": t, "value": M / (t * 1e-3), "unit": UNIT}
+        if not args.no_accuracy:
+            p.forward(F, out=f_out)
+            p.synchronize()
+            e_fwd, e_adj, nsub, _ = subset_accuracy(f_out, F, f, x1, x2, N1, N2, 65536, 7,
+                                                    {"sigma": wl["sigma"], "K": K}, stream, torch)
+            entry.update(rel_l2_forward=e_fwd, rel_l2_adjoint=e_adj, subset_points=nsub)
+        out[f"w{K}"] = entry
+        p.close()
+    return out
 
 
 def run_ours(args, wl):
@@ -653,6 +806,19 @@ def run_ours(args, wl):
                  "note": "cuFFT 2D plan on the same grid with the separate pad / halo fill / halo fold / crop "
                          "kernels; the line's own FFT is the fused passes"}
 
+    study = None
+    if wl["name"].startswith("clustered") and not args.no_precision_study:
+        study = precision_study(args, wl, [k for k in (4, 6, 8) if k != wl["K"]], x1, x2, F, f, stream, flush,
+                                torch)
+        study[f"w{wl['K']}"] = {"ms_per_step": t_step, "value": M / (t_step * 1e-3), "unit": UNIT}
+        if accuracy is not None:
+            study[f"w{wl['K']}"].update(rel_l2_forward=accuracy["rel_l2_forward"],
+                                        rel_l2_adjoint=accuracy["rel_l2_adjoint"],
+                                        subset_points=accuracy["subset_points"])
+        study = dict(sorted(study.items()))
+
+    small = spread_small_cases(stream) if rank == 0 and not args.no_reference_gpu else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl)
@@ -679,6 +845,8 @@ def run_ours(args, wl):
                                         "ms_per_step": t_step + set_points_ms,
                                         "note": "binning timed by the plan's events, plus one execute step"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
+            "precision_study": study,
+            "spread_small_cases": small,
             "gpu_launches": 6 * args.steps,
             "gpu_launches_note": ("our kernels in the timed region per step: column FFT+pad, row FFT+fill, gather, "
                                   "spread, fold+row FFT, column FFT+crop") if fused else
@@ -809,6 +977,7 @@ def knab_cpu_baseline(wl, target_s: float = 15.0, steps: int | None = None):
         b = max((t - t2) / ((rows - r2) * L2), 0.0)
         a = max(t - b * rows * L2, 0.0)
         out["value"] = M / (a + b * M)
+        out["extrapolated"] = True
         out["model"] = {"fixed_s": a, "per_point_s": b, "small_sample_points": r2 * L2, "small_sample_ms": t2 * 1e3}
         how = f"the first {rows} and {r2} of {L1} output rows (x {L2})"
     else:
@@ -1064,11 +1233,15 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="polar")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="clustered")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip timing the reference's own GPU spreading (oracle/_ref)")
+    ap.add_argument("--no-precision-study", action="store_true",
+                    help="clustered workload: skip the other window half-widths (w 4, 6, 8)")
     ap.add_argument("--fft-mode", choices=["auto", "cufft", "pruned", "fused"], default="auto",
                     help="oversampled FFT: auto (fused passes below 2048^2 cells, else cuFFT), cuFFT 2D plan, "
                          "cuFFT passes, fused")

@@ -28,6 +28,8 @@ def test_reference_arm_line():
     assert d["config"]["workload"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["extrapolated"] is False  # config 1 runs every point
+    assert "reference_gpu_spread" in d  # timed on a GPU box, "unavailable" here
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
 

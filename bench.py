@@ -63,7 +63,8 @@ L2_FLUSH_BYTES = 256 << 20
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-def polar_raster(seed: int = 2, spokes: int = 512, samples: int = 2048, N: int = 512, jitter: float = 1e-3):
+def polar_raster(seed: int = 2, spokes: int = 512, samples: int = 2048, N: int = 512, jitter: float = 1e-3,
+                 K: int = 6):
     rng = np.random.default_rng(seed)
     theta = np.pi * np.arange(spokes) / spokes
     r = -0.5 + np.arange(samples) / samples
@@ -74,11 +75,11 @@ def polar_raster(seed: int = 2, spokes: int = 512, samples: int = 2048, N: int =
     x2 = np.mod(x2 + 0.5, 1.0) - 0.5
     F = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))).astype(np.complex64)
     f = (rng.standard_normal(x1.size) + 1j * rng.standard_normal(x1.size)).astype(np.complex64)
-    return dict(name="polar_raster_512x512_1M", N1=N, N2=N, sigma=2.0, K=6,
+    return dict(name="polar_raster_512x512_1M" + ("" if K == 6 else f"_K{K}"), N1=N, N2=N, sigma=2.0, K=K,
                 x1=x1.astype(np.float32), x2=x2.astype(np.float32), F=F, f=f,
                 config={"workload": "polar-raster NFFT (SAR back-projection shape)", "N": [N, N],
                         "points": int(x1.size), "spokes": spokes, "samples_per_spoke": samples,
-                        "jitter": jitter, "sigma": 2.0, "w": 6, "taps": "13x13", "seed": seed})
+                        "jitter": jitter, "sigma": 2.0, "w": K, "taps": f"{2 * K + 1}x{2 * K + 1}", "seed": seed})
 
 
 def uniform_config1(seed: int = 0):
@@ -1247,11 +1248,13 @@ def main():
                          "cuFFT passes, fused")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
-    ap.add_argument("--K", type=int, default=None, help="window half-width for the clustered workload (4, 6, 8)")
+    ap.add_argument("--K", type=int, default=None,
+                    help="window half-width for the clustered and polar workloads (2..8; default 6)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    wl = WORKLOADS[args.workload](K=args.K) if (args.workload == "clustered" and args.K) else WORKLOADS[args.workload]()
+    wl = (WORKLOADS[args.workload](K=args.K) if (args.workload in ("clustered", "polar") and args.K)
+          else WORKLOADS[args.workload]())
     if args.workload == "knab":
         if args.impl == "reference":
             run_knab_reference(args, wl)

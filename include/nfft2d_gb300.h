@@ -33,7 +33,8 @@
  * and never exits the process.  Transforms are asynchronous on the plan's
  * stream; device-side faults that a kernel detects itself (a bounded wait
  * that ran out, a corrupted bin record) are latched in the plan and
- * reported by nfft2d_synchronize().
+ * reported by the next nfft2d_synchronize(), which then clears them: each
+ * such error is reported once, and a later correct run reports NFFT2D_OK.
  */
 #ifndef NFFT2D_GB300_H
 #define NFFT2D_GB300_H
@@ -206,6 +207,10 @@ int nfft2d_device_count(void);
  * the call returns NFFT2D_ERR_DEVICE_TIMEOUT with the context intact.
  * Synchronizes `stream`. */
 int nfft2d_selftest_wait_timeout(int spin_limit, void *stream);
+/* The same bounded wait enqueued on a plan's stream, latching its timeout in
+ * the plan's status word as the plan's own kernels do: the next
+ * nfft2d_synchronize returns NFFT2D_ERR_DEVICE_TIMEOUT (once).  Asynchronous. */
+int nfft2d_plan_selftest_wait_timeout(nfft2d_plan plan, int spin_limit);
 
 /* ---- exact direct sum ----------------------------------------------------
  * Matrix-free FP64 replacement of NDFT2_2D_GPU (NFFT/NDFT2_2D.cu:37-72):
@@ -251,15 +256,19 @@ int nfft2d_batch_adjoint(nfft2d_batch batch, const void *const *f, void *const *
  * once. */
 int nfft2d_batch_spread_ref(nfft2d_batch batch, const void *const *f, void *const *F);
 int nfft2d_batch_set_graph(nfft2d_batch batch, int on);
+/* Waits for the batch's work and reports a latched device-side error once
+ * (cleared after it is read), as nfft2d_synchronize does for plans. */
 int nfft2d_batch_synchronize(nfft2d_batch batch);
+/* Bounded-wait self-test on the batch's stream; the next
+ * nfft2d_batch_synchronize returns NFFT2D_ERR_DEVICE_TIMEOUT (once). */
+int nfft2d_batch_selftest_wait_timeout(nfft2d_batch batch, int spin_limit);
 
 /* ---- forward transform that allocates nothing ----------------------------
  * No counterpart in the reference: an addition for callers that must not
  * allocate device memory while they run -- a host application that owns all
  * device memory through its own pool (a MATLAB MEX gateway working on
- * gpuArray data, for instance), a latency-critical loop that cannot afford
- * cudaMalloc's implicit synchronisation, or code launched inside a CUDA-graph
- * stream capture, where cudaMalloc is not permitted.
+ * gpuArray data, for instance), or a latency-critical loop that cannot afford
+ * cudaMalloc's implicit synchronisation.
  *
  * Same result as nfft2d_forward on a plan (N1, N2, sigma = 2, K), computed
  * without a plan: f_p = sum_k F_k exp(-2 pi i (k1 x1_p / N1 + k2 x2_p / N2)).
@@ -271,9 +280,15 @@ int nfft2d_batch_synchronize(nfft2d_batch batch);
  * device array inside the library (held on each GPU that loads it until the
  * process exits); no cudaMalloc, cudaFree or allocating library call is made.
  * The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make it before any stream capture begins.  All
- * calls share the array: calls that overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller. */
+ * (cudaGetSymbolAddress) and caches it for the life of the process, so make
+ * it before any stream capture begins; a cudaDeviceReset (or other teardown
+ * of the device's primary context) invalidates the cached address, and the
+ * entry point must not be called again in that process afterwards.  All
+ * calls share the array and it keeps the last call's contents: calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  The call reads no status back from the GPU: a
+ * non-finite coordinate gives NaN for that point's output (no error code),
+ * where a plan's set_points would return NFFT2D_ERR_NONFINITE. */
 int nfft2d_forward_small_noalloc(int N1, int N2, int K, long long M, const float *x1, const float *x2, int units,
                                  const void *F, void *f, void *stream);
 

@@ -111,6 +111,7 @@ _SIGNATURES = {
     "nfft2d_status_string": (ctypes.c_char_p, [_I]),
     "nfft2d_device_count": (_I, []),
     "nfft2d_selftest_wait_timeout": (_I, [_I, _P]),
+    "nfft2d_plan_selftest_wait_timeout": (_I, [_P, _I]),
     "nfft2d_ndft2d_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _LL, _LL, _I, _P]),
     "nfft2d_forward_small_noalloc": (_I, [_I, _I, _I, _LL, _P, _P, _I, _P, _P, _P]),
     "nfft2d_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _P, _D, _I, _P]),
@@ -122,6 +123,7 @@ _SIGNATURES = {
     "nfft2d_batch_spread_ref": (_I, [_P, _P, _P]),
     "nfft2d_batch_set_graph": (_I, [_P, _I]),
     "nfft2d_batch_synchronize": (_I, [_P]),
+    "nfft2d_batch_selftest_wait_timeout": (_I, [_P, _I]),
     "nfft2d_knab_window": (_I, [_D, _D, _I, _I, _P, _I, ctypes.POINTER(_I)]),
     "nfft2d_knab_create": (_I, [ctypes.POINTER(_P), _I, _I, _P, _P, _D, _D, _I, _P]),
     "nfft2d_knab_destroy": (_I, [_P]),

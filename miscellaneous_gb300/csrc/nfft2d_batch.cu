@@ -43,7 +43,7 @@ constexpr int kSpreadItem = 128;
 // One transform of a batch, device resident (the tensor map needs 64-byte
 // alignment; the struct keeps it first and the array is allocated aligned).
 struct alignas(128) BatchDesc {
-    CUtensorMap tmap;
+    CUtensorMap tmap;   // the grid with the spread's strip-patch box
     const Rec32 *recs;
     const int4 *chunks;
     float2 *grid;
@@ -225,15 +225,16 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     k_batch_spread(const BatchDesc *__restrict__ d, int first, int n, const BatchIO *__restrict__ io, int chunk0,
                    int total, Geom g0, const __grid_constant__ WinPoly wp, int chunk, int *work, int *status) {
     extern __shared__ unsigned char smem_raw[];
-    constexpr int PR = kRegTile + 2 * K;
-    constexpr int SP = point_scratch<K>();
-    float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    using S = SpreadGeo<K>;
+    unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                                            ~uintptr_t(127));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pstride = patch_stride_elems(g0);
-    float2 *patch = bufs + warp * pstride;
-    float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * SP;
+    float2 *bufs = reinterpret_cast<float2 *>(base) + warp * S::NBUF * S::PATCH;
+    float *scr = reinterpret_cast<float *>(reinterpret_cast<float2 *>(base) + kSpreadWarps * S::NBUF * S::PATCH) +
+                 warp * 32 * S::SP;
     const int parts = (chunk + kSpreadItem - 1) / kSpreadItem;
-    bool pending = false;
+    StripFlush fs{nullptr, bufs, g0.H, 0};
+    strip_flush_init<K>(fs);
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(work, 1);
@@ -249,13 +250,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
         ch.y += first;
         ch.z = min(kSpreadItem, ch.z - first);
         const int tr = ch.x / D.g.tiles2, tc = ch.x - tr * D.g.tiles2;
-        const int r0 = tr * kRegTile, c0 = tc * kRegTile;
-        float2 acc[PR];
-#pragma unroll
-        for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
-        spread_points<K>(D.recs, ch.y, ch.z, r0, c0, io[t].in, scr, acc, wp, status);
-        flush_patch<K>(&D.tmap, patch, acc, g0.H, r0, c0, pending);
-        pending = true;
+        fs.map = &D.tmap;  // this transform's grid (strip-patch box)
+        spread_item<K>(D.recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, io[t].in, scr, fs, wp, status);
     }
     if (lane == 0) bulk_wait_all();
 }
@@ -370,9 +366,7 @@ int launch_gather(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg) {
 template <int K>
 int launch_spread(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg, int sms) {
     if (kg.total_chunks == 0) return NFFT2D_OK;
-    const int pstride = patch_stride_elems(kg.g0);
-    const int smem = kSpreadWarps * pstride * static_cast<int>(sizeof(float2)) + 128 +
-                     kSpreadWarps * 32 * point_scratch<K>() * static_cast<int>(sizeof(float));
+    const int smem = kSpreadWarps * spread_warp_smem_bytes<K>() + 128;
     auto kernel = k_batch_spread<K>;
     if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
@@ -624,7 +618,7 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
         if (st != NFFT2D_OK) return st;
         BatchDesc &D = h[i];
         std::memset(&D, 0, sizeof(D));
-        std::memcpy(&D.tmap, &p->tmap, sizeof(CUtensorMap));
+        std::memcpy(&D.tmap, &p->tmap_spread, sizeof(CUtensorMap));
         D.recs = static_cast<const Rec32 *>(p->recs);
         D.chunks = p->chunks;
         D.grid = static_cast<float2 *>(p->grid);
@@ -679,8 +673,20 @@ int nfft2d_batch_synchronize(nfft2d_batch b) {
     int hs[4] = {0, 0, 0, 0};
     B_TRY(cudaStreamSynchronize(b->stream));
     B_TRY(cudaMemcpy(hs, b->d_status, sizeof(hs), cudaMemcpyDeviceToHost));
+    // a device-side error is reported once: cleared after it is read
+    if (hs[1]) {
+        B_TRY(cudaMemsetAsync(b->d_status + 1, 0, sizeof(int), b->stream));
+        B_TRY(cudaStreamSynchronize(b->stream));
+    }
     if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
     if (hs[1] & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
+    return NFFT2D_OK;
+}
+
+int nfft2d_batch_selftest_wait_timeout(nfft2d_batch b, int spin_limit) {
+    if (!b || spin_limit < 1) return NFFT2D_ERR_INVALID_ARG;
+    k_selftest_latch<<<1, 32, 0, b->stream>>>(static_cast<uint32_t>(spin_limit), b->d_status);
+    B_TRY(cudaGetLastError());
     return NFFT2D_OK;
 }
 

@@ -59,6 +59,19 @@ struct WinConst {
     double kp;      // K / (1 - exp(-2 alpha K)) = cn * exp(alpha K) / 2
 };
 
+// The FP32 tiled spread splits each 16 x 16 tile into vertical strips of SW
+// columns; a group of G lanes owns the G patch columns a strip's windows can
+// touch (SW + 2K <= G), and 32 / G groups add different points of one strip
+// at once.  The binning orders a tile's cells strip by strip (row-major
+// within a strip) so that a strip's points are contiguous and row-sorted.
+__host__ __device__ constexpr int spread_group_lanes(int K) { return K <= 3 ? 8 : (K <= 7 ? 16 : 32); }
+__host__ __device__ constexpr int pow2_floor(int v) {
+    int p = 1;
+    while (p * 2 <= v) p *= 2;
+    return p;
+}
+__host__ __device__ constexpr int spread_strip_width(int K) { return pow2_floor(spread_group_lanes(K) - 2 * K); }
+
 // Geometry shared by kernels.
 struct Geom {
     int n1, n2;         // oversampled grid
@@ -70,6 +83,7 @@ struct Geom {
     int tiles1, tiles2;
     int PR, PC;         // patch rows / cols (complex elements)
     int Ke;             // K rounded up to even (column halo of a patch)
+    int SW;             // strip width of the in-tile cell order (T: plain row-major)
 };
 
 // Per-stage CUDA events on the plan's stream: ev[2s], ev[2s+1] bracket stage s.
@@ -130,6 +144,7 @@ struct nfft2d_plan_s {
     bool fused_ok = false;                   // twiddle tables of the fused passes are set up
     float2 *tw1 = nullptr, *tw2 = nullptr;   // exp(-2 pi i m / n1), exp(-2 pi i m / n2)
     CUtensorMap tmap;  // 64-byte aligned by its own declaration
+    CUtensorMap tmap_spread;  // box of one strip patch of the FP32 tiled spread
     bool tmap_ok = false;
 
     nfft2d::Timer timer;
@@ -196,6 +211,11 @@ cudaError_t fused_type2_cols(const nfft2d_plan_s *p, int sign, const void *F);
 cudaError_t fused_type2_rows(const nfft2d_plan_s *p, int sign);
 cudaError_t fused_type1_rows(const nfft2d_plan_s *p, int sign);
 cudaError_t fused_type1_cols(const nfft2d_plan_s *p, int sign, void *F);
+
+// One thread waits on an mbarrier phase that nothing completes, gives up
+// after `limit` polls and latches kErrTimeout in status[1] (the self-tests of
+// nfft2d_plan_selftest_wait_timeout / nfft2d_batch_selftest_wait_timeout).
+__global__ void k_selftest_latch(uint32_t limit, int *status);
 
 // Host FP64 helpers shared by the plan and the Knab regridder.
 double bessel_i0_host(double x);

@@ -5,10 +5,8 @@
 // such as creating a cuFFT plan) while it runs.  Typical cases are a host
 // application that owns every device allocation through its own pool and
 // forbids extensions to allocate behind its back (a MATLAB MEX gateway working
-// on gpuArray data is one), latency-critical loops where cudaMalloc's implicit
-// device synchronisation and unbounded run time are not acceptable, and code
-// that launches work while a stream is being captured into a CUDA graph,
-// where cudaMalloc is not permitted.
+// on gpuArray data is one), and latency-critical loops where cudaMalloc's
+// implicit device synchronisation and unbounded run time are not acceptable.
 //
 // How: every work buffer -- the padded oversampled grid, the row-transform
 // intermediate and the two deapodization tables -- lives in ONE file-scope
@@ -22,7 +20,10 @@
 // Host code cannot pass the array's name to a kernel (in host code it is a
 // host-side stand-in, not a device address), so the device address is taken
 // with cudaGetSymbolAddress once per device, on the first call made with that
-// device current, and cached.
+// device current, and cached.  The cache lives as long as the process: a
+// cudaDeviceReset (or any other teardown of the device's primary context)
+// reloads the module and may move the array, after which this entry point
+// must not be called again in the same process.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -182,7 +183,9 @@ __global__ void k_na_halo(float2 *__restrict__ grid, int n1, int n2, int C) {
 
 // Gather without binning: each thread reduces its point's coordinates in FP64
 // (v = s x, mu = rint(v) wrapped into [0, n), t = v - mu) and sums its
-// (2K+1)^2 taps from the halo-padded grid.  A non-finite coordinate yields NaN
+// (2K+1)^2 taps from the halo-padded grid: FMA row partials, the weighted row
+// partials summed with TwoSum and the rounding errors carried in a second
+// accumulator, as the plan's gathers do.  A non-finite coordinate yields NaN
 // for that point and reads nothing.
 template <int K>
 __global__ void k_na_gather(const float *__restrict__ x1, const float *__restrict__ x2, int M, double s1,
@@ -206,7 +209,7 @@ __global__ void k_na_gather(const float *__restrict__ x1, const float *__restric
     nfft2d::weights_f32<K>(static_cast<float>(v1 - m1), w1, alpha, cn, kp);
     nfft2d::weights_f32<K>(static_cast<float>(v2 - m2), w2, alpha, cn, kp);
     const float2 *base = grid + static_cast<size_t>(i1 + kHalo - K) * C + (i2 + kHalo - K);
-    float sx = 0.f, sy = 0.f;
+    float sx = 0.f, sy = 0.f, ex = 0.f, ey = 0.f;
 #pragma unroll
     for (int a = 0; a < W; ++a) {
         float rx = 0.f, ry = 0.f;
@@ -216,10 +219,13 @@ __global__ void k_na_gather(const float *__restrict__ x1, const float *__restric
             rx = fmaf(w2[b], u.x, rx);
             ry = fmaf(w2[b], u.y, ry);
         }
-        sx = fmaf(w1[a], rx, sx);
-        sy = fmaf(w1[a], ry, sy);
+        float e;
+        nfft2d::two_sum(sx, __fmul_rn(w1[a], rx), sx, e);
+        ex = __fadd_rn(ex, e);
+        nfft2d::two_sum(sy, __fmul_rn(w1[a], ry), sy, e);
+        ey = __fadd_rn(ey, e);
     }
-    out[p] = make_float2(sx, sy);
+    out[p] = make_float2(sx + ex, sy + ey);
 }
 
 template <int K>

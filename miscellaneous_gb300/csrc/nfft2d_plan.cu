@@ -279,6 +279,15 @@ int make_tensor_map(nfft2d_plan_s *p) {
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return NFFT2D_ERR_CUDA;
+    // the spread's strip patch: G lane columns (+2 for odd K, whose patch
+    // starts one column early to keep the box on a 16-byte boundary)
+    const int K = (g.PR - g.T) / 2;
+    cuuint32_t sbox[2] = {static_cast<cuuint32_t>(2 * (spread_group_lanes(K) + 2 * (K & 1))),
+                          static_cast<cuuint32_t>(g.PR)};
+    r = enc(&p->tmap_spread, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, p->grid, dims, strides, sbox, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return NFFT2D_ERR_CUDA;
     p->tmap_ok = true;
     return NFFT2D_OK;
 }
@@ -452,7 +461,9 @@ __device__ __forceinline__ int wrap_index(long long m, int n) {
 // t = v - mu in [-1/2, 1/2] (NFFT2_2D.cu:167-173 does the same in the data
 // precision).  FP32 coordinates with a power-of-two scale and no origin take
 // an exact FP32 path (the product, rint and the difference are all exact);
-// everything else is reduced in FP64.
+// everything else -- including a finite coordinate whose FP32 product is too
+// large for that path -- is reduced in FP64.  Only a non-finite coordinate is
+// rejected.
 template <typename CT, typename TT>
 __device__ __forceinline__ bool reduce_coord(CT x, double o, double s, float sf, bool exact_f32, int n, int &mu,
                                              TT &t) {
@@ -464,7 +475,6 @@ __device__ __forceinline__ bool reduce_coord(CT x, double o, double s, float sf,
             mu = wrap_index(static_cast<long long>(m), n);
             return true;
         }
-        if (!isfinite(v)) return false;
     }
     double v = (static_cast<double>(x) - o) * s;
     if (!isfinite(v)) return false;
@@ -497,8 +507,12 @@ __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2
         mu1 = mu2 = 0;
         r.t1 = r.t2 = 0;
     }
+    // cell key: tile, then strip, row and column within the strip
     const int tr = mu1 / g.T, tc = mu2 / g.T;
-    const unsigned key = (static_cast<unsigned>(tr * g.tiles2 + tc) * g.T + (mu1 - tr * g.T)) * g.T + (mu2 - tc * g.T);
+    const int lr = mu1 - tr * g.T, lc = mu2 - tc * g.T;
+    const int st = lc / g.SW, sc = lc - st * g.SW;
+    const unsigned key = static_cast<unsigned>(tr * g.tiles2 + tc) * static_cast<unsigned>(g.T * g.T) +
+                         static_cast<unsigned>((st * g.T + lr) * g.SW + sc);
     const unsigned rank = atomicAdd(cell_count + key, 1u);
     r.mu = (mu1 << 16) | mu2;
     r.orig = static_cast<int>(key);
@@ -839,6 +853,23 @@ __global__ void k_selftest_wait(uint32_t limit) {
     }
 }
 
+}  // namespace
+
+namespace nfft2d {
+// The same bounded wait latching kErrTimeout into a plan's (or batch's)
+// status word, as the tiled kernels do when their own wait runs out.
+__global__ void k_selftest_latch(uint32_t limit, int *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_proxy_async_smem();
+        if (!mbar_wait_bounded(&bar, 0, limit)) latch_error(status, kErrTimeout);
+    }
+}
+}  // namespace nfft2d
+
+namespace {
+
 // Launch shape for the small elementwise kernels.
 dim3 row_grid(int cols, int rows) {
     const int bx = std::max(1, std::min((cols + 255) / 256, 64));
@@ -880,6 +911,9 @@ int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile,
     g->tiles1 = (g->n1 + T - 1) / T;
     g->tiles2 = (g->n2 + T - 1) / T;
     g->Ke = K + (K & 1);
+    // strip-major cell order inside a tile where the register spread runs
+    // (FP32, 16 x 16 tiles), plain row-major elsewhere
+    g->SW = (precision == NFFT2D_F32 && T == 16) ? spread_strip_width(K) : T;
     g->PR = T + 2 * K;
     // Patch row pitch: the T + 2Ke columns a tile needs, rounded up to 16
     // complex (128 bytes); with it a warp's reads of one tap spread over the
@@ -1559,8 +1593,19 @@ int nfft2d_synchronize(nfft2d_plan p) {
         if (hs[0] < 0 || hs[0] > p->chunks_cap) return NFFT2D_ERR_INTERNAL;
         p->n_chunks = hs[0];
     }
-    if (hs[1] & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
-    if (hs[1] & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
+    // a device-side error is reported once: the bits are cleared after
+    // they are read (the stream is idle here)
+    const int bits = hs[1];
+    if (bits) NFFT_TRY_CUDA(cudaMemsetAsync(p->d_status + 1, 0, sizeof(int), p->stream));
+    if (bits & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
+    if (bits & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
+    return NFFT2D_OK;
+}
+
+int nfft2d_plan_selftest_wait_timeout(nfft2d_plan p, int spin_limit) {
+    if (!p || spin_limit < 1) return NFFT2D_ERR_INVALID_ARG;
+    nfft2d::k_selftest_latch<<<1, 32, 0, p->stream>>>(static_cast<uint32_t>(spin_limit), p->d_status);
+    NFFT_TRY_CUDA(cudaGetLastError());
     return NFFT2D_OK;
 }
 

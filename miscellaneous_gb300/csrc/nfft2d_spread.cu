@@ -5,17 +5,19 @@
 // issues 338 global float atomics per point).
 //
 // TILED variant (FP32 plans, 16 x 16 tiles): a warp pulls work items
-// (tile, point range) from a global counter and accumulates the tile's
-// (16+2K) x 32 patch IN REGISTERS: lane l owns patch column l and holds the
-// patch rows of that column.  The warp walks its points one at a time; every
-// lane reads the point's row weights (broadcast) and its own column weight
-// from a per-warp scratch and adds to the 2K+1 rows starting at the point's
-// row offset (a warp-uniform switch keeps the register indices static).  No
-// shared-memory or global atomics: the patch leaves once per work item, lanes
-// -> shared memory -> ONE TMA tensor reduction (cp.reduce.async.bulk.tensor
-// .2d ... .add, f32) into the padded grid, overlapped with the next item.  The
-// halo of the padded grid is folded back onto the interior afterwards
-// (k_halo_fold), so no kernel wraps indices.
+// (tile, point range) from a global counter.  The binning orders a tile's
+// points by vertical strip (SW columns, 4 at K = 6) and by row within a
+// strip; the warp splits into groups of G lanes (16 at K = 6) whose lane l
+// owns column l of the strip's patch -- every column the strip's windows
+// can touch -- IN REGISTERS, one float2 per patch row.  The groups add
+// different points of one row run at once with packed FP32x2 FMAs
+// (static register indices: the run's row is warp-uniform), so 2K+1 of G
+// lanes do useful work.  No shared-memory or global atomics: when the strip
+// changes, the groups' patches are summed by warp shuffles and leave through
+// shared memory as ONE TMA tensor reduction (cp.reduce.async.bulk.tensor.2d
+// ... .add, f32) into the padded grid, double-buffered so that the next
+// strip overlaps it.  The halo of the padded grid is folded back onto the
+// interior afterwards (k_halo_fold), so no kernel wraps indices.
 //
 // Why not shared-memory atomics: on this GPU a float atomicAdd to shared
 // memory runs as a compare-and-swap loop (measured ~470 instructions per
@@ -48,18 +50,19 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
                                                                     const float2 *__restrict__ f,
                                                                     const __grid_constant__ KArgs a) {
     extern __shared__ unsigned char smem_raw[];
-    constexpr int PR = kRegTile + 2 * K;  // patch rows
-    const Geom g = a.g;                   // g.T == kRegTile, g.PC == 32
+    using S = SpreadGeo<K>;
+    const Geom g = a.g;  // g.T == kRegTile, g.SW == S::SW
     // TMA shared-memory operands: 128-byte aligned (the launch adds 128 bytes of slack)
-    float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                                            ~uintptr_t(127));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pstride = patch_stride_elems(g);
-    float2 *patch = bufs + warp * pstride;  // this warp's flush buffer, PR x 32
-    constexpr int SP = point_scratch<K>();
-    float *scr = reinterpret_cast<float *>(bufs + kSpreadWarps * pstride) + warp * 32 * SP;
+    float2 *bufs = reinterpret_cast<float2 *>(base) + warp * S::NBUF * S::PATCH;
+    float *scr = reinterpret_cast<float *>(reinterpret_cast<float2 *>(base) + kSpreadWarps * S::NBUF * S::PATCH) +
+                 warp * 32 * S::SP;
     const int n = a.n_chunks >= 0 ? a.n_chunks : a.status[0];  // < 0: counted on the device only
     int *work = a.status + 2;  // work-item counter, zeroed before the launch
-    bool pending = false;
+    StripFlush fs{&tmap, bufs, g.H, 0};
+    strip_flush_init<K>(fs);
 
     const int parts = (a.chunk + kSpreadItem - 1) / kSpreadItem;  // items per chunk
     for (;;) {
@@ -74,14 +77,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
         ch.y += first;
         ch.z = min(kSpreadItem, ch.z - first);
         const int tr = ch.x / g.tiles2, tc = ch.x - tr * g.tiles2;
-        const int r0 = tr * kRegTile, c0 = tc * kRegTile;
-
-        float2 acc[PR];
-#pragma unroll
-        for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
-        spread_points<K>(recs, ch.y, ch.z, r0, c0, f, scr, acc, a.poly, a.status);
-        flush_patch<K>(&tmap, patch, acc, g.H, r0, c0, pending);
-        pending = true;
+        spread_item<K>(recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, f, scr, fs, a.poly, a.status);
     }
     if (lane == 0) bulk_wait_all();
 }
@@ -126,10 +122,9 @@ template <int K>
 cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
     const KArgs a = make_kargs(p);
     if (p->precision == NFFT2D_F32 && p->spread_variant == NFFT2D_VARIANT_TILED && p->g.T == kRegTile &&
-        p->g.PC == 32) {
+        p->g.SW == SpreadGeo<K>::SW) {
         if (p->n_chunks == 0) return cudaSuccess;
-        const int smem = kSpreadWarps * patch_stride_elems(p->g) * static_cast<int>(sizeof(float2)) + 128 +
-                         kSpreadWarps * 32 * point_scratch<K>() * static_cast<int>(sizeof(float));
+        const int smem = kSpreadWarps * spread_warp_smem_bytes<K>() + 128;
         auto kernel = k_spread_tiled<K>;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -143,7 +138,7 @@ cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
             const int need = static_cast<int>((items + kSpreadWarps - 1) / kSpreadWarps);
             if (blocks > need) blocks = need;
         }
-        kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(p->tmap, static_cast<const Rec32 *>(p->recs),
+        kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(p->tmap_spread, static_cast<const Rec32 *>(p->recs),
                                                                 p->chunks, static_cast<const float2 *>(f), a);
         return cudaGetLastError();
     }

@@ -115,54 +115,63 @@ __device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ g
 }
 
 // ---------------------------------------------------------------------------
-// spread: a warp accumulates a 16 x 16 tile's (16+2K) x 32 patch in registers
+// spread: lane groups accumulate a tile strip's patch in registers
 // ---------------------------------------------------------------------------
+// A work item holds points of one 16 x 16 tile, ordered strip by strip (SW
+// columns each, spread_strip_width) and by row within a strip.  The warp
+// splits into 32/G groups of G lanes; lane l of every group owns patch column
+// l of the current strip, i.e. grid column c0 + s*SW - K + l, for the 16+2K
+// patch rows (acc[r], one float2 per row).  A point at strip column q touches
+// patch columns q .. q+2K, all inside the group, so 2K+1 of G lanes do useful
+// work (13 of 16 at K = 6) where a lane-per-tile-column layout keeps 13 of 32.
+// The groups take different points of the same row run at once (the static
+// register indices need a warp-uniform row), and their partial patches are
+// added by warp shuffles when the strip is flushed: lanes -> shared patch ->
+// one TMA tensor reduction (f32 add) into the grid.
 constexpr int kRegTile = 16;  // tile edge the register-resident spread requires
 
-// Per-point scratch (floats): lr, lc, v.x, v.y; the row weights w1 padded to
-// a multiple of 4 floats (2K+1 used); then the column products v * w2 as
-// float2, same padding.  The stride between points is kept off multiples of
-// 8 floats: the prepass has every lane write its own point, and a stride with
-// a larger power-of-two factor maps more lanes onto one bank (at K = 8 the
-// unpadded 64 put all 32 lanes on one bank).
 template <int K>
-constexpr int wpad() {
-    return ((2 * K + 1 + 3) / 4) * 4;
-}
+struct SpreadGeo {
+    static constexpr int W = 2 * K + 1;
+    static constexpr int G = spread_group_lanes(K);     // lanes per group
+    static constexpr int NG = 32 / G;                   // groups per warp
+    static constexpr int SW = spread_strip_width(K);    // strip width (columns)
+    static constexpr int NS = kRegTile / SW;            // strips per tile
+    static constexpr int PR = kRegTile + 2 * K;         // patch rows
+    static constexpr int ODD = K & 1;                   // odd K: box starts one column early
+    static constexpr int BOXC = G + 2 * ODD;            // shared patch / TMA box columns (complex)
+    static constexpr int NBUF = NS > 1 ? 2 : 1;         // flush buffers per warp
+    static constexpr int W1 = ((W + 3) / 4) * 4;        // floats of the row weights (padded)
+    static constexpr int WV = ((2 * W + 3) / 4) * 4;    // floats of the column products v * w2
+    // per-point scratch (floats): {lr, strip column, strip, -}, the row
+    // weights, the column products as float2.  The stride is 4 mod 8: the
+    // prepass's 16-byte stores of 8 consecutive lanes hit 8 distinct bank
+    // quads, and the groups' loads of consecutive points hit distinct banks.
+    // (A shared-memory load costs about one wavefront per float it delivers
+    // whatever its width, so the row weights are stored once and broadcast.)
+    static constexpr int SP0 = 4 + W1 + WV;
+    static constexpr int SP = SP0 % 8 == 0 ? SP0 + 4 : SP0;
+    static constexpr int PATCH = ((PR * BOXC + 15) / 16) * 16;  // float2 per buffer, 128-byte multiple
+    static_assert(SW + 2 * K <= G, "strip windows must fit the group");
+    static_assert(kRegTile % SW == 0, "strips tile the tile");
+};
+
+// Shared memory of one spreading warp: NBUF patch buffers + the point scratch.
 template <int K>
-constexpr int point_scratch() {
-    return (4 + 3 * wpad<K>()) % 8 == 0 ? 4 + 3 * wpad<K>() + 4 : 4 + 3 * wpad<K>();
+__host__ __device__ constexpr int spread_warp_smem_bytes() {
+    using S = SpreadGeo<K>;
+    return S::NBUF * S::PATCH * 8 + 32 * S::SP * 4;
 }
 
 // acc[L + a] += (ax, ay) * w1[a] for the 2K+1 rows of a point whose first
 // patch row is L (compile-time, so acc stays in registers).
 template <int K, int PR, int L>
-__device__ __forceinline__ void add_rows(float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax, float ay) {
+__device__ __forceinline__ void add_rows2(float2 (&acc)[PR], const float (&w1)[2 * K + 1], float2 v) {
 #pragma unroll
     for (int a = 0; a <= 2 * K; ++a) {
-        acc[L + a].x = fmaf(ax, w1[a], acc[L + a].x);
-        acc[L + a].y = fmaf(ay, w1[a], acc[L + a].y);
+        acc[L + a].x = fmaf(v.x, w1[a], acc[L + a].x);
+        acc[L + a].y = fmaf(v.y, w1[a], acc[L + a].y);
     }
-}
-
-// Dispatch on the point's first patch row with a jump table (the row offset
-// is warp-uniform, so every lane takes the same case).
-template <int K, int PR>
-__device__ __forceinline__ void add_rows_switch(int lr, float2 (&acc)[PR], const float (&w1)[wpad<K>()], float ax,
-                                                float ay) {
-    static_assert(kRegTile == 16, "one case per row of a 16-row tile");
-#define NFFT2D_ROW_CASE(L)                   \
-    case L:                                  \
-        add_rows<K, PR, L>(acc, w1, ax, ay); \
-        break;
-    switch (lr) {
-        NFFT2D_ROW_CASE(0) NFFT2D_ROW_CASE(1) NFFT2D_ROW_CASE(2) NFFT2D_ROW_CASE(3)
-        NFFT2D_ROW_CASE(4) NFFT2D_ROW_CASE(5) NFFT2D_ROW_CASE(6) NFFT2D_ROW_CASE(7)
-        NFFT2D_ROW_CASE(8) NFFT2D_ROW_CASE(9) NFFT2D_ROW_CASE(10) NFFT2D_ROW_CASE(11)
-        NFFT2D_ROW_CASE(12) NFFT2D_ROW_CASE(13) NFFT2D_ROW_CASE(14) NFFT2D_ROW_CASE(15)
-        default: break;
-    }
-#undef NFFT2D_ROW_CASE
 }
 
 // f(integral_constant<int, L>) for L = 0, 1, ..., in order.
@@ -171,24 +180,93 @@ __device__ __forceinline__ void for_each_row(F &&f, std::integer_sequence<int, L
     (f(std::integral_constant<int, Ls>{}), ...);
 }
 
-// Add the contributions of points [first, first + cnt) of one tile (origin
-// r0, c0) to the warp's register patch acc (lane = patch column).  scr is the
-// warp's scratch of 32 * point_scratch<K>() floats.  A record outside the tile
+// cp.async.bulk.wait_group.read N: at most N of the thread's bulk groups are
+// still reading their shared-memory source.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Per-warp flush state of the strip spread.
+struct StripFlush {
+    const CUtensorMap *map;  // the grid's strip-patch tensor map
+    float2 *bufs;            // NBUF patch buffers of this warp
+    int H;                   // grid halo
+    int issued;              // flushes issued so far by this warp
+};
+
+// Zero the warp's patch buffers once (odd K: the columns outside the lanes
+// stay zero for the life of the kernel).
+template <int K>
+__device__ __forceinline__ void strip_flush_init(StripFlush &fs) {
+    using S = SpreadGeo<K>;
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < S::NBUF * S::PATCH; i += 32) fs.bufs[i] = make_float2(0.f, 0.f);
+    __syncwarp();
+}
+
+// Add the groups' partial patches, write the strip patch to the next flush
+// buffer and reduce it into the grid with one TMA tensor reduction at strip
+// s of the tile with origin (r0, c0).
+template <int K>
+__device__ __forceinline__ void strip_flush(StripFlush &fs, float2 (&acc)[SpreadGeo<K>::PR], int r0, int c0, int s) {
+    using S = SpreadGeo<K>;
+    const int lane = threadIdx.x & 31;
+    if constexpr (S::NG > 1) {
+#pragma unroll
+        for (int r = 0; r < S::PR; ++r) {
+#pragma unroll
+            for (int off = 16; off >= S::G; off >>= 1) {
+                acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, off);
+                acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, off);
+            }
+        }
+    }
+    float2 *buf = fs.bufs + (fs.issued % S::NBUF) * S::PATCH;
+    // the reduction that last read this buffer has finished reading it
+    if (lane == 0 && fs.issued >= S::NBUF) {
+        if constexpr (S::NBUF == 2)
+            asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        else
+            bulk_wait_read_all();
+    }
+    __syncwarp();
+    if (lane < S::G) {
+#pragma unroll
+        for (int r = 0; r < S::PR; ++r) buf[r * S::BOXC + S::ODD + lane] = acc[r];
+    }
+    fence_proxy_async_smem();  // generic-proxy writes -> visible to the TMA engine
+    __syncwarp();
+    if (lane == 0) {
+        tma_reduce_add_2d(fs.map, buf, 2 * (fs.H + c0 + s * S::SW - K - S::ODD), fs.H + r0 - K);
+        bulk_commit();
+    }
+    ++fs.issued;
+}
+
+// Spread points [first, first + cnt) of one tile (origin r0, c0) into the
+// grid, strip by strip, flushing each strip's register patch.  scr is the
+// warp's scratch of 32 * SpreadGeo<K>::SP floats.  A record outside the tile
 // latches kErrBounds and contributes nothing.
 template <int K>
-__device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, int first, int cnt, int r0, int c0,
-                                              const float2 *__restrict__ f, float *scr,
-                                              float2 (&acc)[kRegTile + 2 * K], const WinPoly &wp, int *status) {
-    constexpr int W = 2 * K + 1;
-    constexpr int PR = kRegTile + 2 * K;
-    constexpr int KE = K + (K & 1);
-    constexpr int SP = point_scratch<K>(), WP = wpad<K>();
+__device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int first, int cnt, int r0, int c0,
+                                            const float2 *__restrict__ f, float *scr, StripFlush &fs,
+                                            const WinPoly &wp, int *status) {
+    using S = SpreadGeo<K>;
+    constexpr int W = S::W, PR = S::PR, SP = S::SP, W1 = S::W1, WV = S::WV;
     const int lane = threadIdx.x & 31;
+    const int grp = lane / S::G, gl = lane % S::G;
+    float2 acc[PR];
+#pragma unroll
+    for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
+    int cur = -1;  // strip held in acc
+    // each batch's records are loaded one batch ahead (the next batch's load
+    // overlaps this batch's walk)
+    int4 raw_next = make_int4(0, 0, 0, 0);
+    if (lane < cnt) raw_next = __ldg(reinterpret_cast<const int4 *>(recs) + first + lane);
     for (int base0 = 0; base0 < cnt; base0 += 32) {
         const int nb = min(32, cnt - base0);
+        const int4 raw = raw_next;
         // 1) each lane prepares one point: offsets, value, 2(2K+1) weights
+        int my_key = 0x7fffffff;  // (strip << 4) | row, sorted ascending along the batch
         if (lane < nb) {
-            const int4 raw = __ldg(reinterpret_cast<const int4 *>(recs) + first + base0 + lane);
             const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
             int lr = mu1 - r0, lc = mu2 - c0;
             float2 v = __ldg(&f[raw.w]);
@@ -198,114 +276,93 @@ __device__ __forceinline__ void spread_points(const Rec32 *__restrict__ recs, in
                 lr = lc = 0;
                 v = make_float2(0.f, 0.f);  // contributes nothing
             }
+            const int st = lc / S::SW;
+            my_key = (st << 4) | lr;
             float w1[W], w2[W];
             weights_poly<K>(__int_as_float(raw.x), w1, wp);
             weights_poly<K>(__int_as_float(raw.y), w2, wp);
             float *sp = scr + lane * SP;
-            reinterpret_cast<float4 *>(sp)[0] = make_float4(__int_as_float(lr), __int_as_float(lc), v.x, v.y);
+            reinterpret_cast<int4 *>(sp)[0] = make_int4(lr, lc - st * S::SW, st, 0);
+            float4 *wq = reinterpret_cast<float4 *>(sp + 4);
 #pragma unroll
-            for (int k = 0; k < WP; ++k) sp[4 + k] = k < W ? w1[k] : 0.f;
+            for (int k = 0; k < W1 / 4; ++k)
+                wq[k] = make_float4(w1[4 * k], 4 * k + 1 < W ? w1[4 * k + 1] : 0.f,
+                                    4 * k + 2 < W ? w1[4 * k + 2] : 0.f, 4 * k + 3 < W ? w1[4 * k + 3] : 0.f);
+            float4 *vq = reinterpret_cast<float4 *>(sp + 4 + W1);
 #pragma unroll
-            for (int k = 0; k < WP; ++k)
-                reinterpret_cast<float2 *>(sp + 4 + WP)[k] =
-                    k < W ? make_float2(v.x * w2[k], v.y * w2[k]) : make_float2(0.f, 0.f);
-        }
-        __syncwarp();
-        // 2) the warp walks the points; lane = patch column.  Operands of
-        //    point j: the 2K+1 row weights (broadcast) and this lane's column
-        //    product v * w2 (zero outside the point's columns).
-        auto load = [&](int j, float (&w1)[WP], float &ax, float &ay) {
-            const float *sp = scr + j * SP;
-            const int lc = __float_as_int(sp[1]);
-#pragma unroll
-            for (int q = 0; q < WP / 4; ++q) {
-                const float4 t = reinterpret_cast<const float4 *>(sp + 4)[q];
-                w1[4 * q] = t.x;
-                w1[4 * q + 1] = t.y;
-                w1[4 * q + 2] = t.z;
-                w1[4 * q + 3] = t.w;
+            for (int k = 0; k < WV / 4; ++k) {
+                const float a = 2 * k < W ? w2[2 * k] : 0.f;
+                const float b = 2 * k + 1 < W ? w2[2 * k + 1] : 0.f;
+                vq[k] = make_float4(v.x * a, v.y * a, v.x * b, v.y * b);
             }
-            const int b = lane - lc - (KE - K);  // this lane's tap column
-            const float2 vw = (static_cast<unsigned>(b) < static_cast<unsigned>(W))
-                                  ? reinterpret_cast<const float2 *>(sp + 4 + WP)[b] : make_float2(0.f, 0.f);
-            ax = vw.x;
-            ay = vw.y;
+        }
+        if (base0 + 32 + lane < cnt) raw_next = __ldg(reinterpret_cast<const int4 *>(recs) + first + base0 + 32 + lane);
+        __syncwarp();
+        // 2) operands of point p for this lane: the row weights (broadcast
+        //    within the group) and this lane's column product (zero outside
+        //    the point's columns, or when the group has no point this step)
+        auto load = [&](int p, bool ok, float (&w1)[W], float2 &vw) {
+            const float *sp = scr + p * SP;
+            const float4 *wq = reinterpret_cast<const float4 *>(sp + 4);
+#pragma unroll
+            for (int k = 0; k < W / 4; ++k) {
+                const float4 t = wq[k];
+                w1[4 * k] = t.x;
+                w1[4 * k + 1] = t.y;
+                w1[4 * k + 2] = t.z;
+                w1[4 * k + 3] = t.w;
+            }
+#pragma unroll
+            for (int a = (W / 4) * 4; a < W; ++a) w1[a] = sp[4 + a];
+            const int b = gl - reinterpret_cast<const int *>(sp)[1];
+            vw = (ok && static_cast<unsigned>(b) < static_cast<unsigned>(W))
+                     ? reinterpret_cast<const float2 *>(sp + 4 + W1)[b] : make_float2(0.f, 0.f);
         };
-        int j = 0;
-        // The binning sorts a tile's points by row, so the walk visits the
-        // row offsets in increasing order: phase L adds its run of points to
-        // acc[L .. L+2K] with compile-time register indices and no indirect
-        // branch.  A point out of order -- only after a latched bounds error
-        // -- is left to the dispatch loop below.  From K = 6 up each run is
-        // counted by one ballot; for narrower windows comparing each next
-        // point's row measured faster (2-3x at K <= 5 on GB300).
-        if constexpr (K < 6) {
-            int lr_j = nb > 0 ? __float_as_int(scr[0]) : kRegTile;
+        // The binning keeps a work item's keys ascending; a batch out of
+        // order can only follow a record that failed the bounds check above
+        // (already latched): it is skipped rather than given a slow path of
+        // its own (16 more copies of the row update would not fit the
+        // instruction cache alongside the walk).
+        const int prev = __shfl_up_sync(0xffffffffu, my_key, 1);
+        const bool sorted = __all_sync(0xffffffffu, lane == 0 || lane >= nb || prev <= my_key);
+        if (!sorted && lane == 0) latch_error(status, kErrBounds);
+        int j = sorted ? 0 : nb;
+        while (j < nb) {
+            const int st = __shfl_sync(0xffffffffu, my_key, j) >> 4;
+            if (st != cur) {
+                if (cur >= 0) {
+                    strip_flush<K>(fs, acc, r0, c0, cur);
+#pragma unroll
+                    for (int r = 0; r < PR; ++r) acc[r] = make_float2(0.f, 0.f);
+                }
+                cur = st;
+            }
+            // the strip's points, row run by row run: run L adds to
+            // acc[L .. L+2K] with compile-time register indices, NG
+            // points of the run per step; rows without points are
+            // skipped by one mask test
+            const unsigned rows =
+                __reduce_or_sync(0xffffffffu, (my_key >> 4) == st ? (1u << (my_key & 15)) : 0u);
             for_each_row(
                 [&](auto Lc) {
                     constexpr int L = decltype(Lc)::value;
-                    // two points per iteration: 2-3 us faster per 2^20 points at
-                    // K = 2..5 (unrolling the ballot walk of K >= 6 was slower)
-#pragma unroll 2
-                    while (lr_j == L) {
-                        float w1[WP], ax, ay;
-                        load(j, w1, ax, ay);
-                        ++j;
-                        lr_j = j < nb ? __float_as_int(scr[j * SP]) : kRegTile;
-                        add_rows<K, PR, L>(acc, w1, ax, ay);
+                    if (!(rows & (1u << L))) return;
+                    const int n = __popc(__ballot_sync(0xffffffffu, my_key == ((st << 4) | L)));
+#pragma unroll 1
+                    for (int k = 0; k < n; k += S::NG) {
+                        const bool ok = k + grp < n;
+                        float w1[W];
+                        float2 vw;
+                        load(ok ? j + k + grp : j, ok, w1, vw);
+                        add_rows2<K, PR, L>(acc, w1, vw);
                     }
+                    j += n;
                 },
                 std::make_integer_sequence<int, kRegTile>{});
-        } else {
-            const int my_lr = lane < nb ? __float_as_int(scr[lane * SP]) : kRegTile;
-            const int prev = __shfl_up_sync(0xffffffffu, my_lr, 1);
-            const bool sorted = __all_sync(0xffffffffu, lane == 0 || prev <= my_lr);
-            if (sorted) {
-                for_each_row(
-                    [&](auto Lc) {
-                        constexpr int L = decltype(Lc)::value;
-                        const int e = j + __popc(__ballot_sync(0xffffffffu, my_lr == L));
-                        for (; j < e; ++j) {
-                            float w1[WP], ax, ay;
-                            load(j, w1, ax, ay);
-                            add_rows<K, PR, L>(acc, w1, ax, ay);
-                        }
-                    },
-                    std::make_integer_sequence<int, kRegTile>{});
-            }
-        }
-        for (; j < nb; ++j) {
-            float w1[WP], ax, ay;
-            load(j, w1, ax, ay);
-            add_rows_switch<K, PR>(__float_as_int(scr[j * SP]), acc, w1, ax, ay);
         }
         __syncwarp();  // scratch is rewritten by the next batch
     }
-}
-
-// cp.async.bulk.wait_group.read 0: the thread's last bulk reduction has
-// finished reading its shared-memory source.
-__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-
-// Flush a warp's register patch: lanes -> shared patch (PR x 32) -> one TMA
-// tensor reduction into the grid at the tile (r0, c0).  `pending` tells
-// whether the warp's previous flush may still be reading the patch.
-template <int K>
-__device__ __forceinline__ void flush_patch(const CUtensorMap *map, float2 *patch, const float2 (&acc)[kRegTile + 2 * K],
-                                            int H, int r0, int c0, bool pending) {
-    constexpr int PR = kRegTile + 2 * K;
-    constexpr int KE = K + (K & 1);
-    const int lane = threadIdx.x & 31;
-    if (lane == 0 && pending) bulk_wait_read_all();
-    __syncwarp();
-#pragma unroll
-    for (int r = 0; r < PR; ++r) patch[r * 32 + lane] = acc[r];
-    fence_proxy_async_smem();  // generic-proxy writes -> visible to the TMA engine
-    __syncwarp();
-    if (lane == 0) {
-        tma_reduce_add_2d(map, patch, 2 * (H + c0 - KE), H + r0 - K);
-        bulk_commit();
-    }
+    if (cur >= 0) strip_flush<K>(fs, acc, r0, c0, cur);
 }
 
 }  // namespace nfft2d

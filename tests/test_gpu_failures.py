@@ -88,3 +88,61 @@ def test_bounded_device_wait_reports_timeout():
                       torch.zeros(M, dtype=torch.complex64, device=dev))
     a = a.cpu().numpy()
     assert np.linalg.norm(a - exact) / np.linalg.norm(exact) < 1e-5  # the FP32 bar
+
+
+def test_latched_timeout_is_reported_once_then_clears():
+    """A bounded wait that runs out on a plan's (and a batch's) stream latches
+    a timeout in its status word; the next synchronize reports it and clears
+    it, so a correct run afterwards reports OK and gives right results."""
+    from miscellaneous_gb300 import _lib
+    from miscellaneous_gb300.nfft import Batch, Plan
+    lib = _lib.load()
+    dev = "cuda:0"
+    g = torch.Generator(device=dev).manual_seed(21)
+    N, M = 32, 500
+    x1 = torch.rand(M, device=dev, generator=g) - 0.5
+    x2 = torch.rand(M, device=dev, generator=g) - 0.5
+    F = torch.randn(N * N, dtype=torch.complex64, device=dev, generator=g)
+    with Plan(N, N) as p:
+        p.set_points(x1, x2)
+        ref = p.forward(F)
+        p.synchronize()
+        assert lib.nfft2d_plan_selftest_wait_timeout(p.handle, 0) == _lib.ERR_INVALID_ARG
+        assert lib.nfft2d_plan_selftest_wait_timeout(p.handle, 1000) == 0
+        with pytest.raises(_lib.NFFT2DError) as e:
+            p.synchronize()
+        assert e.value.status == _lib.ERR_DEVICE_TIMEOUT
+        out = p.forward(F)
+        p.synchronize()  # reported once: a good run afterwards is OK
+        torch.testing.assert_close(out, ref, rtol=0, atol=0)
+    with Batch([(N, N), (16, 16)]) as b:
+        b.set_points([x1, x1[:100].contiguous()], [x2, x2[:100].contiguous()])
+        b.synchronize()
+        assert lib.nfft2d_batch_selftest_wait_timeout(b._h, 1000) == 0
+        with pytest.raises(_lib.NFFT2DError) as e:
+            b.synchronize()
+        assert e.value.status == _lib.ERR_DEVICE_TIMEOUT
+        outs = b.forward([F, F[:256].contiguous()])
+        b.synchronize()
+        # batch (direct gather) vs plan (tiled gather): FP32 rounding only
+        assert (torch.linalg.vector_norm(outs[0] - ref) / torch.linalg.vector_norm(ref)).item() < 1e-6
+
+
+def test_huge_finite_coordinates_are_reduced_not_rejected():
+    """A finite FP32 coordinate whose FP32 product with the (power-of-two)
+    scale overflows is reduced in FP64 like any other; only NaN and +-Inf
+    are rejected."""
+    from miscellaneous_gb300 import _lib
+    from miscellaneous_gb300.nfft import Plan
+    dev = "cuda:0"
+    x1 = torch.tensor([0.1, 3.0e38, -2.5e38, 0.25], dtype=torch.float32, device=dev)
+    x2 = torch.tensor([0.2, 0.3, 1.0e37, -0.4], dtype=torch.float32, device=dev)
+    with Plan(16, 16) as p:
+        p.set_points(x1, x2)  # units "unit": the scale sigma * N = 32 is a power of two; x * 32 overflows FP32
+        F = torch.randn(256, dtype=torch.complex64, device=dev)
+        f = p.forward(F)
+        p.synchronize()
+        assert torch.isfinite(torch.view_as_real(f)).all()
+        with pytest.raises(_lib.NFFT2DError) as e:
+            p.set_points(torch.tensor([0.1, float("inf")], device=dev), torch.tensor([0.0, 0.0], device=dev))
+        assert e.value.status == _lib.ERR_NONFINITE

@@ -13,11 +13,11 @@
 // different points of one row run at once with packed FP32x2 FMAs
 // (static register indices: the run's row is warp-uniform), so 2K+1 of G
 // lanes do useful work.  No shared-memory or global atomics: when the strip
-// changes, the groups' patches are summed by warp shuffles and leave through
-// shared memory as ONE TMA tensor reduction (cp.reduce.async.bulk.tensor.2d
-// ... .add, f32) into the padded grid, double-buffered so that the next
-// strip overlaps it.  The halo of the padded grid is folded back onto the
-// interior afterwards (k_halo_fold), so no kernel wraps indices.
+// changes, each group's patch leaves through shared memory as one TMA tensor
+// reduction (cp.reduce.async.bulk.tensor.2d ... .add, f32) into the padded
+// grid, which runs while the warp walks the next strip.  The halo of the
+// padded grid is folded back onto the interior afterwards (k_halo_fold), so
+// no kernel wraps indices.
 //
 // Why not shared-memory atomics: on this GPU a float atomicAdd to shared
 // memory runs as a compare-and-swap loop (measured ~470 instructions per

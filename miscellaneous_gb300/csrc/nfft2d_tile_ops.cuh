@@ -125,9 +125,10 @@ __device__ __forceinline__ float2 gather_direct_f32(const float2 *__restrict__ g
 // patch columns q .. q+2K, all inside the group, so 2K+1 of G lanes do useful
 // work (13 of 16 at K = 6) where a lane-per-tile-column layout keeps 13 of 32.
 // The groups take different points of the same row run at once (the static
-// register indices need a warp-uniform row), and their partial patches are
-// added by warp shuffles when the strip is flushed: lanes -> shared patch ->
-// one TMA tensor reduction (f32 add) into the grid.
+// register indices need a warp-uniform row); when the strip is flushed each
+// group's patch goes lanes -> its own shared patch -> one TMA tensor
+// reduction (f32 add) into the grid (the TMA engine adds the groups'
+// patches; no shuffles).
 constexpr int kRegTile = 16;  // tile edge the register-resident spread requires
 
 template <int K>
@@ -140,7 +141,7 @@ struct SpreadGeo {
     static constexpr int PR = kRegTile + 2 * K;         // patch rows
     static constexpr int ODD = K & 1;                   // odd K: box starts one column early
     static constexpr int BOXC = G + 2 * ODD;            // shared patch / TMA box columns (complex)
-    static constexpr int NBUF = NS > 1 ? 2 : 1;         // flush buffers per warp
+    static constexpr int NBUF = NG;                     // flush buffers per warp: one per group
     static constexpr int W1 = ((W + 3) / 4) * 4;        // floats of the row weights (padded)
     static constexpr int WV = ((2 * W + 3) / 4) * 4;    // floats of the column products v * w2
     // per-point scratch (floats): {lr, strip column, strip, -}, the row
@@ -202,40 +203,26 @@ __device__ __forceinline__ void strip_flush_init(StripFlush &fs) {
     __syncwarp();
 }
 
-// Add the groups' partial patches, write the strip patch to the next flush
-// buffer and reduce it into the grid with one TMA tensor reduction at strip
-// s of the tile with origin (r0, c0).
+// Write each group's patch to its own shared buffer and reduce them into the
+// grid with one TMA tensor reduction per group at strip s of the tile with
+// origin (r0, c0).  Lane 0 issues every reduction, so its bulk-group wait
+// covers the buffers' previous readers.
 template <int K>
 __device__ __forceinline__ void strip_flush(StripFlush &fs, float2 (&acc)[SpreadGeo<K>::PR], int r0, int c0, int s) {
     using S = SpreadGeo<K>;
     const int lane = threadIdx.x & 31;
-    if constexpr (S::NG > 1) {
-#pragma unroll
-        for (int r = 0; r < S::PR; ++r) {
-#pragma unroll
-            for (int off = 16; off >= S::G; off >>= 1) {
-                acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, off);
-                acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, off);
-            }
-        }
-    }
-    float2 *buf = fs.bufs + (fs.issued % S::NBUF) * S::PATCH;
-    // the reduction that last read this buffer has finished reading it
-    if (lane == 0 && fs.issued >= S::NBUF) {
-        if constexpr (S::NBUF == 2)
-            asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-        else
-            bulk_wait_read_all();
-    }
+    // the reductions issued by the previous flush have finished reading
+    if (lane == 0 && fs.issued > 0) bulk_wait_read_all();
     __syncwarp();
-    if (lane < S::G) {
+    float2 *buf = fs.bufs + (lane / S::G) * S::PATCH;
 #pragma unroll
-        for (int r = 0; r < S::PR; ++r) buf[r * S::BOXC + S::ODD + lane] = acc[r];
-    }
+    for (int r = 0; r < S::PR; ++r) buf[r * S::BOXC + S::ODD + (lane % S::G)] = acc[r];
     fence_proxy_async_smem();  // generic-proxy writes -> visible to the TMA engine
     __syncwarp();
     if (lane == 0) {
-        tma_reduce_add_2d(fs.map, buf, 2 * (fs.H + c0 + s * S::SW - K - S::ODD), fs.H + r0 - K);
+        const int x = 2 * (fs.H + c0 + s * S::SW - K - S::ODD), y = fs.H + r0 - K;
+#pragma unroll
+        for (int g = 0; g < S::NG; ++g) tma_reduce_add_2d(fs.map, fs.bufs + g * S::PATCH, x, y);
         bulk_commit();
     }
     ++fs.issued;

@@ -1,14 +1,18 @@
 """nfft2d_forward_small_noalloc: the forward transform for callers that may
 not allocate device memory while they run (a host that owns every device
-allocation through its own pool, a latency-critical loop, code launched
-inside a CUDA-graph stream capture).  Its work buffers live in one fixed
-device array inside the library instead of memory it allocates.
+allocation through its own pool, such as a MEX gateway working on gpuArray
+data, or a latency-critical loop that cannot take cudaMalloc's implicit
+synchronisation).  Its work buffers live in one fixed device array inside
+the library instead of memory it allocates.
 
 Checked through the C ABI against the existing plan entry point
 nfft2d_forward on the same inputs, on two calls in a row (the second with
 different inputs, so stale contents of the shared array would show), and
-against the FP64 NDFT.  Tolerance: rel-L2 <= 1e-5, the bar the other FP32
-tests use against the FP64 NDFT.  This file is collected last on purpose.
+against the FP64 NDFT, in grid, unit and radian coordinates.  Tolerance:
+rel-L2 <= 1e-5, the bar the other FP32 tests use against the FP64 NDFT.
+After a first call has loaded the kernels, further calls leave the device's
+free memory and torch's allocation count unchanged.  This file is collected
+last on purpose.
 """
 import ctypes
 
@@ -31,7 +35,15 @@ def _case(N1, N2, M, seed, units="unit"):
     if units == "grid":
         x1 = (x1 * N1).astype(np.float32)
         x2 = (x2 * N2).astype(np.float32)
+    elif units == "radians":
+        x1 = (x1 * 2 * np.pi).astype(np.float32)
+        x2 = (x2 * 2 * np.pi).astype(np.float32)
     return F, x1, x2
+
+
+def _grid_units(x, N, units):
+    x = x.astype(np.float64)
+    return {"grid": x, "unit": x * N, "radians": x * N / (2 * np.pi)}[units]
 
 
 def _noalloc(lib, N1, N2, K, F, x1, x2, units):
@@ -59,7 +71,7 @@ def _plan_forward(N1, N2, K, F, x1, x2, units):
 
 
 @pytest.mark.parametrize("N1,N2,K,M,units", [(64, 48, 6, 3000, "unit"), (128, 128, 6, 20000, "grid"),
-                                             (16, 32, 4, 777, "unit")])
+                                             (16, 32, 4, 777, "unit"), (32, 64, 5, 1500, "radians")])
 def test_noalloc_forward_matches_plan_forward_twice(lib, orc, N1, N2, K, M, units):
     for call, seed in enumerate((100 + N1, 200 + N2)):  # two calls in a row, different inputs
         F, x1, x2 = _case(N1, N2, M, seed, units)
@@ -67,8 +79,7 @@ def test_noalloc_forward_matches_plan_forward_twice(lib, orc, N1, N2, K, M, unit
         want = _plan_forward(N1, N2, K, F, x1, x2, units)
         assert np.all(np.isfinite(got)), f"call {call}"
         assert orc.rel_l2(got, want) < 1e-5, f"call {call}"
-        g1 = x1.astype(np.float64) * (N1 if units == "unit" else 1)
-        g2 = x2.astype(np.float64) * (N2 if units == "unit" else 1)
+        g1, g2 = _grid_units(x1, N1, units), _grid_units(x2, N2, units)
         exact = orc.ndft_type2(F.astype(np.complex128), g1, g2, sign=-1)
         assert orc.rel_l2(got, exact) < 1e-5, f"call {call}"
 
@@ -84,3 +95,27 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
     assert lib.nfft2d_forward_small_noalloc(64, 64, 9, 0, z, z, 1, z, z, z) == _lib.ERR_INVALID_ARG
     assert lib.nfft2d_forward_small_noalloc(4, 4, 6, 0, z, z, 1, z, z, z) == _lib.ERR_INVALID_ARG
     assert "scratch" in _lib.status_string(_lib.ERR_SCRATCH_LIMIT)
+
+
+def test_noalloc_call_allocates_no_device_memory(lib):
+    """After a warm-up call (kernel loading may allocate once), a call leaves
+    the device's free memory and torch's allocator untouched."""
+    from miscellaneous_gb300 import _lib
+    dev = "cuda:0"
+    F, x1, x2 = _case(96, 96, 5000, 7)
+    tF, t1, t2 = (torch.from_numpy(a).to(dev) for a in (F, x1, x2))
+    out = torch.empty(x1.size, dtype=torch.complex64, device=dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def call():
+        st = lib.nfft2d_forward_small_noalloc(96, 96, 6, x1.size, _ptr(t1), _ptr(t2), _lib.UNITS["unit"], _ptr(tF),
+                                              _ptr(out), stream)
+        assert st == 0, _lib.status_string(st)
+        torch.cuda.synchronize()
+
+    call()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for _ in range(3):
+        call()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0

@@ -175,8 +175,42 @@ def pso_batch(seed: int = 6, count: int = 250, N: int = 44, M: int = 44 * 44):
                         "seed": seed})
 
 
+def ffbp_scene(seed: int = 7, Np: int = 64, nf: int = 216, Nx: int = 128, step: float = 0.08, R: float = 10e3):
+    """The reference's SAR scenario (BP_FBP_FFBP_main.m:7-103): a straight
+    track at R = 10 km and 30 degrees depression, a 3-degree aperture,
+    216 frequency samples over 600 MHz at 10 GHz, a 128 x 128 scene at 8 cm
+    -- with 64 pulses instead of 128 (the 128-pulse recursion asks its Knab
+    regridding for an odd NFFT grid that the reference's NFFT1_2D cannot take).
+    Three unit point targets at seeded positions in the scene."""
+    rng = np.random.default_rng(seed)
+    c, fc, BW = 299792458.0, 10e9, 600e6
+    deltaF = BW / nf
+    minF = fc - BW / 2.0
+    f2 = minF + nf * deltaF
+    maxAz, dep = 3 * math.pi / 180, math.pi / 6
+    az = np.arange(Np) / Np * maxAz - maxAz / 2
+    X = R * math.cos(dep) * np.ones(Np)
+    Y = R * math.cos(dep) * np.tan(az)
+    Z = R * math.sin(dep) * np.ones(Np)
+    R0 = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    W = Nx * step
+    v = np.linspace(-W / 2, W / 2, Nx)
+    x_mat, y_mat = np.meshgrid(v, v)
+    targets = [(0.0, 0.0)] + [tuple(t) for t in rng.uniform(-0.4 * W, 0.4 * W, (2, 2))]
+    fk = minF + np.arange(nf) * deltaF
+    ph = np.zeros((nf, Np), dtype=np.complex128)
+    for tx, ty in targets:
+        dR = np.sqrt((X - tx) ** 2 + (Y - ty) ** 2 + Z ** 2) - R0
+        ph += np.exp(-1j * 4 * math.pi * np.outer(fk, dR) / c)
+    data = dict(AntX=X, AntY=Y, AntZ=Z, R0=R0, phdata=ph, x_mat=x_mat, y_mat=y_mat, z_mat=np.zeros_like(x_mat))
+    return dict(name=f"ffbp_{Np}pulses_{nf}f_{Nx}x{Nx}", data=data, sar=dict(c=c, fc=fc, BW=BW, f2=f2), Np=Np,
+                config={"workload": "FFBP SAR image formation (knabNFFT2D regridding, NFFT1_1D leaves)",
+                        "pulses": Np, "frequency_samples": nf, "scene": [Nx, Nx], "pixel_m": step, "range_m": R,
+                        "targets": len(targets), "seed": seed})
+
+
 WORKLOADS = {"polar": polar_raster, "config1": uniform_config1, "clustered": clustered_config3, "batch": uneven_batch,
-             "lsq": least_squares_config5, "knab": knab_regrid, "pso": pso_batch}
+             "lsq": least_squares_config5, "knab": knab_regrid, "pso": pso_batch, "ffbp": ffbp_scene}
 
 
 # ---------------------------------------------------------------------------
@@ -1228,6 +1262,96 @@ def run_batch(args, wl):
     batch.close()
 
 
+FFBP_METRIC = "FFBP SAR image: NU points/s (leaf NFFT1_1D points + Knab-regridded points) per image"
+
+
+def ffbp_cpu_rate():
+    """The oracle's restated FFBP (oracle/ffbp.py, FP64, OpenMP C kernels) on
+    an 8-pulse, 64-sample, 32 x 32 point-target scene: points per second
+    counted as the library counts them."""
+    import oracle
+    from oracle import ffbp as F
+    oracle.build()
+    data, sar = F.point_target_scene(Np=8, nf=64, Nx=32, R=2e3, step=0.08)
+    import torch
+    pts = None
+    if torch.cuda.is_available():  # the work count of the same scene, from the library
+        from miscellaneous_gb300.sar import FFBP
+        st = {}
+        FFBP(data, 1, 8, c=sar["c"], fc=sar["fc"], BW=sar["BW"], f2=sar["f2"], precision="f64", stats=st)
+        pts = st["leaf_points"] + st["regrid_points"]
+    F.ffbp(data, sar, 1, 8)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        F.ffbp(data, sar, 1, 8)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return {"seconds_per_image": t, "points": pts, "value": (pts / t) if pts else None, "unit": UNIT,
+            "cores": oracle.get_threads(), "kind": "port", "extrapolated": False,
+            "sample": "8 pulses, 64 frequency samples, 32 x 32 scene at 2 km (the largest 8-pulse scene the "
+                      "reference's recursion can run), median of 3 images; oracle/ffbp.py over the C restatements "
+                      "of knabNFFT2D.m and NFFT1_1D.m"}
+
+
+def run_ffbp(args, wl):
+    import torch
+
+    from miscellaneous_gb300.sar import FFBP, polar_grid
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    data, sar, Np = wl["data"], wl["sar"], wl["Np"]
+    rho, cosa = polar_grid(data, 1)
+    kw = dict(c=sar["c"], fc=sar["fc"], BW=sar["BW"], f2=sar["f2"], stream=stream)
+    dev_data = dict(data, phdata=torch.from_numpy(data["phdata"]).to(dev))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st = {}
+    for _ in range(args.warmup):
+        FFBP(dev_data, 1, Np, precision="f32", stats=st, **kw)
+    torch.cuda.synchronize()
+    ms = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            ev0.record(stream)
+            im = FFBP(dev_data, 1, Np, precision="f32", **kw)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+    t = statistics.median(ms)
+    pts = st["leaf_points"] + st["regrid_points"]
+    im64 = FFBP(dev_data, 1, Np, precision="f64", **kw)
+    a, b = im.to(torch.complex128), im64
+    m = ~torch.isnan(b.real)
+    err = float(torch.linalg.vector_norm((a - b)[m]) / torch.linalg.vector_norm(b[m]))
+    cpu = None if args.no_cpu_baseline else ffbp_cpu_rate()
+    line = {"metric": FFBP_METRIC, "value": pts / (t * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": wl["config"], "work": st,
+            "images_per_s": 1e3 / t,
+            "accuracy": {"rel_l2_f32_vs_f64": err, "nan_pixels": int((~m).sum()),
+                         "note": "FP32 data (FP64 coordinates and phases) against the library's FP64 image; the FP64 "
+                                 "path matches the oracle's restated recursion to 2e-12 (tests/test_gpu_ffbp.py)"},
+            "cpu_baseline": cpu, "clocks": clocks.summary(),
+            "step": "one whole image: host recursion, plan and regridder set-up, every kernel (CUDA events around "
+                    "the synchronous call)"}
+    print(json.dumps(line))
+
+
+def run_ffbp_reference(args, wl):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cb = ffbp_cpu_rate()
+    value = cb["value"] if cb["value"] is not None else 1.0 / cb["seconds_per_image"]
+    line = {"impl": "reference", "metric": FFBP_METRIC, "value": value,
+            "unit": UNIT if cb["value"] is not None else "images/s", "n_gpus": world, "steps": 3,
+            "warmup": 1, "ms_per_step": cb["seconds_per_image"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl["config"], "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1255,6 +1379,12 @@ def main():
         args.warmup = 3
     wl = (WORKLOADS[args.workload](K=args.K) if (args.workload in ("clustered", "polar") and args.K)
           else WORKLOADS[args.workload]())
+    if args.workload == "ffbp":
+        if args.impl == "reference":
+            run_ffbp_reference(args, wl)
+        else:
+            run_ffbp(args, wl)
+        return
     if args.workload == "knab":
         if args.impl == "reference":
             run_knab_reference(args, wl)

@@ -352,6 +352,57 @@ int nfft2d_knab_nfft2d(double extrap_re, double extrap_im, const double *rho_in,
                        int Nrows, const void *data, const double *rho_out, const double *cos_out, int len1, int len2,
                        double B1, double B2, int precision, void *out, void *stream);
 
+/* ---- fast factorized back-projection (FFBP) -------------------------------
+ * Replaces the NFFT-interpolated branch of BP_FBP_FFBP/FFBP_POLAR_NFFT.m:1-158
+ * (with BP_POLAR_NFFT.m:1-25 and NFFT1_1D.m at the leaves): the SAR image of
+ * pulses a..b (0-based, inclusive) at len1 x len2 output points given in the
+ * polar frame of antenna a (rho_out: range from antenna a; cos_out: cosine of
+ * the angle to the track direction; FFBP.m:10-22 builds them from a Cartesian
+ * scene).  The aperture is split in two at floor((a + b) / 2) until at most
+ * three pulses remain; each half's image is formed on its own polar raster
+ * (sample counts and padded axes as FFBP_POLAR_NFFT.m:58-64), brought to
+ * baseband, regridded onto the parent's points by the Knab-window NFFT
+ * interpolator (knabNFFT2D, extrapolation NaN) and re-modulated; the two
+ * halves are summed.  A leaf back-projects each pulse through a 1D type-2
+ * NFFT of its nf frequency samples (sigma 2, K 6).
+ *
+ *   sar               propagation speed, centre frequency fc, bandwidth and
+ *                     maximum frequency f2 (the reference's globals c, fc,
+ *                     BW, f2);
+ *   ant_x/y/z, r0     np antenna positions and reference ranges, HOST arrays
+ *                     (a straight track, as the recursion's polar shift
+ *                     assumes);
+ *   phdata            np x nf complex (pulse n's samples at phdata[n nf + k],
+ *                     the reference's data.phdata column n), DEVICE;
+ *   rho_out, cos_out  len1 x len2 FP64, DEVICE;  image: len1 x len2 complex,
+ *                     DEVICE.
+ * Complex data are float2 for NFFT2D_F32 (coordinates and phases are always
+ * FP64) and double2 for NFFT2D_F64.  Synchronous on `stream`.  Returns
+ * NFFT2D_ERR_INVALID_ARG where the reference cannot run (a sub-aperture whose
+ * range extent gives fewer than two samples, or a regridding its NFFT1_2D
+ * cannot take, see nfft2d_knab_set_points). */
+typedef struct {
+    double c;       /* propagation speed [m/s]         */
+    double fc;      /* centre frequency [Hz]           */
+    double bw;      /* bandwidth [Hz]                  */
+    double f_max;   /* maximum frequency f2 [Hz]       */
+} nfft2d_sar;
+
+/* Work done by one nfft2d_ffbp_polar call (stats may be NULL). */
+typedef struct {
+    int depth;                  /* levels of the recursion below the top       */
+    int regrids;                /* Knab regriddings                            */
+    int leaves;                 /* leaf back-projections                       */
+    long long leaf_points;      /* points of the leaves' 1D NFFTs (per pulse)  */
+    long long regrid_points;    /* output points of all regriddings            */
+    long long raster_cells;     /* cells of all sub-aperture rasters           */
+} nfft2d_ffbp_stats;
+
+int nfft2d_ffbp_polar(const nfft2d_sar *sar, int np, const double *ant_x, const double *ant_y, const double *ant_z,
+                      const double *r0, int nf, const void *phdata, int a, int b, int len1, int len2,
+                      const double *rho_out, const double *cos_out, int precision, void *image, void *stream,
+                      nfft2d_ffbp_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,6 +83,20 @@ class NFFT2DError(RuntimeError):
         super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
 
 
+class Sar(ctypes.Structure):
+    """nfft2d_sar: propagation speed, centre frequency, bandwidth, maximum frequency."""
+    _fields_ = [("c", ctypes.c_double), ("fc", ctypes.c_double), ("bw", ctypes.c_double), ("f_max", ctypes.c_double)]
+
+
+class FfbpStats(ctypes.Structure):
+    _fields_ = [("depth", ctypes.c_int), ("regrids", ctypes.c_int), ("leaves", ctypes.c_int),
+                ("leaf_points", ctypes.c_longlong), ("regrid_points", ctypes.c_longlong),
+                ("raster_cells", ctypes.c_longlong)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 _P = ctypes.c_void_p
@@ -133,6 +147,8 @@ _SIGNATURES = {
     "nfft2d_knab_synchronize": (_I, [_P]),
     "nfft2d_knab_plan": (_P, [_P]),
     "nfft2d_knab_nfft2d": (_I, [_D, _D, _P, _I, _P, _I, _P, _P, _P, _I, _I, _D, _D, _I, _P, _P]),
+    "nfft2d_ffbp_polar": (_I, [ctypes.POINTER(Sar), _I, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I, _P, _P, _I, _P, _P,
+                               ctypes.POINTER(FfbpStats)]),
 }
 
 

@@ -23,7 +23,11 @@ LIB_NAME = "libnfft2d_gb300.so"
 LIB_PATH = os.path.join(LIB_DIR, LIB_NAME)
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off: host arithmetic rounds as written on every host (the Arm
+# host compiler would otherwise fuse multiply-adds), so host-side sizes and
+# axes match an IEEE restatement bit for bit.
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

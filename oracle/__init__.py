@@ -71,6 +71,7 @@ def _load():
         "oracle_phi": (D, [D, I, D]),
         "oracle_fft2d": (None, [P, L, L, I]),
         "oracle_nfft1_2d": (I, [P, L, L, P, P, L, D, I, I, P]),
+        "oracle_nfft1_1d": (I, [P, L, P, L, D, I, I, P]),
         "oracle_nfft1_2d_grad": (I, [P, L, L, P, P, L, D, I, I, P, P]),
         "oracle_nfft2_2d": (I, [P, P, P, L, L, L, D, I, I, P]),
         "oracle_ndft_type2": (None, [P, L, L, P, P, L, I, P]),
@@ -228,6 +229,18 @@ def rel_l2(a, b) -> float:
     b = np.asarray(b, dtype=np.complex128).ravel()
     den = np.sqrt(np.sum(np.abs(b) ** 2))
     return float(np.sqrt(np.sum(np.abs(a - b) ** 2)) / den) if den > 0 else float(np.sqrt(np.sum(np.abs(a) ** 2)))
+
+
+def nfft1_1d(data, x, c: float = 2.0, K: int = 6, sign: int = -1) -> np.ndarray:
+    """Restated NFFT1_1D.m (BP_FBP_FFBP/NFFT1_1D.m:1-51): the 1D type-2 NFFT
+    of N samples at points x in grid units (period N)."""
+    data = _c128(data).ravel()
+    x = _f64(x).ravel()
+    out = np.zeros(x.size, dtype=np.complex128)
+    rc = _load().oracle_nfft1_1d(_ptr(data), data.size, _ptr(x), x.size, float(c), int(K), int(sign), _ptr(out))
+    if rc != 0:
+        raise ValueError("oracle_nfft1_1d: N must be even and c*N an even integer")
+    return out
 
 
 def conv_window(f: float, B: float, T: float) -> float:

@@ -327,6 +327,50 @@ int oracle_nfft1_2d(const double *F, long N1, long N2, const double *x1, const d
     return 0;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Restated NFFT1_1D (forward, type 2, one dimension): BP_FBP_FFBP/NFFT1_1D.m */
+/* ------------------------------------------------------------------------ */
+/* result_l = sum_k data_k exp(sign 2 pi i k x_l / N), k = -N/2 .. N/2-1, x in
+ * grid units.  Both windows of NFFT1_1D.m are divided by I0(K alpha)
+ * (:16,:30); the factor cancels and is left out. */
+int oracle_nfft1_1d(const double *data, long N, const double *x, long M, double c, int K, int sign, double *out) {
+    long n;
+    if (check_grid(N, c, &n) || K < 1) return -1;
+    const double alpha = oracle_kb_alpha(c);
+    double *phi = deapod_table(N, c, K, alpha); /* :14-16 */
+    /* STEP 1 (:36-37): data ./ phi into the centered block of u */
+    cplx *u = (cplx *)calloc((size_t)n, sizeof(cplx));
+    const cplx *d = (const cplx *)data;
+    const long o = n / 2 - N / 2;
+    for (long i = 0; i < N; ++i) {
+        u[o + i].re = d[i].re / phi[i];
+        u[o + i].im = d[i].im / phi[i];
+    }
+    /* STEP 2 (:43): U = fft(ifftshift(u)); for even n ifftshift swaps halves */
+    cplx *U = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+    for (long k = 0; k < n; ++k) U[k] = u[(k + n / 2) % n];
+    oracle_fft2d((double *)U, 1, n, sign);
+    /* STEP 3 (:22-30, :49-50): (2K+1)-tap windowed gather */
+    cplx *res = (cplx *)out;
+#pragma omp parallel for schedule(static)
+    for (long l = 0; l < M; ++l) {
+        const double mu = matlab_round(c * x[l]);
+        double sr = 0, si = 0;
+        for (int m = -K; m <= K; ++m) {
+            const double w = oracle_phi_hat(c * x[l] - (mu + m), K, alpha);
+            const long r = pos_mod((long)mu + m, n);
+            sr += w * U[r].re;
+            si += w * U[r].im;
+        }
+        res[l].re = sr;
+        res[l].im = si;
+    }
+    free(U);
+    free(u);
+    free(phi);
+    return 0;
+}
+
 /* Derivative of the restated forward w.r.t. the point coordinates (grid
  * units): d f / d x1 = c * sum phi_hat'(c x1 - n1) phi_hat(c x2 - n2) U[n].
  * Same steps 1-2 as oracle_nfft1_2d; step 3 uses the window derivative. */

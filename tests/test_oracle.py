@@ -141,3 +141,28 @@ def test_gradient_oracles(orc):
     assert orc.rel_l2(g1, fd1) < 1e-8 and orc.rel_l2(g2, fd2) < 1e-8
     a1, a2 = orc.nfft1_2d_grad(F, x1, x2)
     assert orc.rel_l2(a1, g1) < 1e-9 and orc.rel_l2(a2, g2) < 1e-9
+
+
+def test_oracle_nfft1_1d_matches_direct_sum(orc):
+    """Restated NFFT1_1D.m (c = 2, K = 6) against the exact 1D sum."""
+    rng = np.random.default_rng(11)
+    N = 216  # the reference's frequency samples per pulse (BP_FBP_FFBP_main.m:16)
+    d = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    x = rng.uniform(-N / 2, N / 2, 300)
+    k = np.arange(N) - N // 2
+    exact = np.exp(-2j * np.pi * np.outer(x, k) / N) @ d
+    assert orc.rel_l2(orc.nfft1_1d(d, x), exact) < 1e-10
+
+
+def test_oracle_ffbp_focuses_a_point_target(orc):
+    """The restated FFBP recursion images a point target at the scene centre,
+    and a geometry with an odd NFFT grid is refused as the reference's
+    NFFT1_2D would refuse it."""
+    from oracle import ffbp as F
+    data, sar = F.point_target_scene(Np=8, nf=64, Nx=32, R=2e3, step=0.08)
+    im = np.nan_to_num(np.abs(F.ffbp(data, sar, 1, 8)))
+    peak = np.unravel_index(np.argmax(im), im.shape)
+    assert all(abs(p - 15.5) <= 1.5 for p in peak)
+    data, sar = F.point_target_scene(Np=16, nf=64, Nx=32, R=2e3, step=0.08)
+    with pytest.raises(ValueError):
+        F.ffbp(data, sar, 1, 16)

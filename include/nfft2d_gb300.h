@@ -352,6 +352,21 @@ int nfft2d_knab_nfft2d(double extrap_re, double extrap_im, const double *rho_in,
                        int Nrows, const void *data, const double *rho_out, const double *cos_out, int len1, int len2,
                        double B1, double B2, int precision, void *out, void *stream);
 
+/* ---- type-3 NUFFT (nonuniform points to nonuniform frequencies) -----------
+ * Replaces NUFFT_2D_CPU (NFFT/NFFT3/C/NFFT3_2D_C.h, NFFT3_2D_C.cpp:199-312),
+ * same argument order:
+ *     F[k] = sum_j f[j] exp(-i (s[k] x[j] + t[k] y[j])),  j < len_in, k < len_out,
+ * by Gaussian gridding at the reference's R = 2.2 and Gaussian width for the
+ * accuracy eps (0 < eps < 1): a spread onto an Mry x Mrx grid sized from the
+ * extents of both point sets, a 2D FFT and a Gaussian gather with the
+ * reference's pre- and post-compensation.  x, y, s, t: FP64 DEVICE arrays;
+ * f, F: DEVICE complex (float2 for NFFT2D_F32, double2 for NFFT2D_F64; the
+ * weights are FP64 either way).  The work grid is allocated per call.
+ * Synchronous on `stream`.  NFFT2D_ERR_INVALID_ARG when all x or all y are
+ * equal (the reference divides by that extent). */
+int nfft2d_nufft3_2d(const double *x, const double *y, const double *s, const double *t, const void *f, void *F,
+                     double eps, long long len_in, long long len_out, int precision, void *stream);
+
 /* ---- fast factorized back-projection (FFBP) -------------------------------
  * Replaces the NFFT-interpolated branch of BP_FBP_FFBP/FFBP_POLAR_NFFT.m:1-158
  * (with BP_POLAR_NFFT.m:1-25 and NFFT1_1D.m at the leaves): the SAR image of

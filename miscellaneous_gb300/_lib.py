@@ -147,6 +147,7 @@ _SIGNATURES = {
     "nfft2d_knab_synchronize": (_I, [_P]),
     "nfft2d_knab_plan": (_P, [_P]),
     "nfft2d_knab_nfft2d": (_I, [_D, _D, _P, _I, _P, _I, _P, _P, _P, _I, _I, _D, _D, _I, _P, _P]),
+    "nfft2d_nufft3_2d": (_I, [_P, _P, _P, _P, _P, _P, _D, _LL, _LL, _I, _P]),
     "nfft2d_ffbp_polar": (_I, [ctypes.POINTER(Sar), _I, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I, _P, _P, _I, _P, _P,
                                ctypes.POINTER(FfbpStats)]),
 }

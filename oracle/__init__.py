@@ -72,6 +72,8 @@ def _load():
         "oracle_fft2d": (None, [P, L, L, I]),
         "oracle_nfft1_2d": (I, [P, L, L, P, P, L, D, I, I, P]),
         "oracle_nfft1_1d": (I, [P, L, P, L, D, I, I, P]),
+        "oracle_ndft3_2d": (None, [P, P, P, L, P, P, L, P]),
+        "oracle_nufft3_2d": (I, [P, P, P, L, P, P, L, D, D, P, P]),
         "oracle_nfft1_2d_grad": (I, [P, L, L, P, P, L, D, I, I, P, P]),
         "oracle_nfft2_2d": (I, [P, P, P, L, L, L, D, I, I, P]),
         "oracle_ndft_type2": (None, [P, L, L, P, P, L, I, P]),
@@ -241,6 +243,29 @@ def nfft1_1d(data, x, c: float = 2.0, K: int = 6, sign: int = -1) -> np.ndarray:
     if rc != 0:
         raise ValueError("oracle_nfft1_1d: N must be even and c*N an even integer")
     return out
+
+
+def ndft3_2d(x, y, f, s, t) -> np.ndarray:
+    """Exact type-3 sum F_k = sum_j f_j exp(-i (s_k x_j + t_k y_j)) (FP64)."""
+    x, y, s, t = (_f64(v).ravel() for v in (x, y, s, t))
+    f = _c128(f).ravel()
+    out = np.zeros(s.size, dtype=np.complex128)
+    _load().oracle_ndft3_2d(_ptr(x), _ptr(y), _ptr(f), x.size, _ptr(s), _ptr(t), s.size, _ptr(out))
+    return out
+
+
+def nufft3_2d(x, y, f, s, t, eps: float, R: float = 2.2):
+    """Restated NUFFT_2D_CPU (NFFT/NFFT3/C/NFFT3_2D_C.cpp:199-312): Gaussian
+    gridding type-3 NUFFT.  Returns (F, {"Mrx", "Mry", "msp"})."""
+    x, y, s, t = (_f64(v).ravel() for v in (x, y, s, t))
+    f = _c128(f).ravel()
+    out = np.zeros(s.size, dtype=np.complex128)
+    info = np.zeros(3, dtype=np.int64)
+    rc = _load().oracle_nufft3_2d(_ptr(x), _ptr(y), _ptr(f), x.size, _ptr(s), _ptr(t), s.size, float(eps), float(R),
+                                  _ptr(out), _ptr(info))
+    if rc != 0:
+        raise ValueError("oracle_nufft3_2d: degenerate input extent")
+    return out, dict(Mrx=int(info[0]), Mry=int(info[1]), msp=int(info[2]))
 
 
 def conv_window(f: float, B: float, T: float) -> float:

@@ -30,6 +30,7 @@
  *       the adjoint identity.
  */
 #include <math.h>
+#include <float.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -652,6 +653,128 @@ void oracle_ndft2_2d_general(const double *X, const double *Y, const double *u, 
         o[q].re = sr;
         o[q].im = si;
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Type-3 2D NUFFT (non-uniform to non-uniform)                              */
+/* ------------------------------------------------------------------------ */
+/* Exact sum F_k = sum_j f_j exp(-i (s_k x_j + t_k y_j)). */
+void oracle_ndft3_2d(const double *x, const double *y, const double *f, long M, const double *s, const double *t,
+                     long N, double *F) {
+    const cplx *fc = (const cplx *)f;
+    cplx *o = (cplx *)F;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < N; ++k) {
+        double sr = 0, si = 0;
+        for (long j = 0; j < M; ++j) {
+            const double ang = -(s[k] * x[j] + t[k] * y[j]);
+            const double cr = cos(ang), ci = sin(ang);
+            sr += fc[j].re * cr - fc[j].im * ci;
+            si += fc[j].re * ci + fc[j].im * cr;
+        }
+        o[k].re = sr;
+        o[k].im = si;
+    }
+}
+
+static double minmax_d(const double *v, long n, int want_max) {
+    double m = want_max ? -FLT_MAX : FLT_MAX; /* the reductions' initial values (:214-232) */
+    for (long i = 0; i < n; ++i) m = want_max ? (v[i] > m ? v[i] : m) : (v[i] < m ? v[i] : m);
+    return m;
+}
+
+/* Restated NUFFT_2D_CPU (NFFT/NFFT3/C/NFFT3_2D_C.cpp:199-312) with its
+ * gridding (:38-85), shifts (:135-151) and spectral gridding with
+ * compensation (:156-194): Gaussian gridding at R = 2.2 for accuracy eps.
+ * R is a parameter (the C++ uses 2.2).  info (may be NULL) receives
+ * Mrx, Mry, msp.  Returns 0, or -1 for a degenerate input extent. */
+int oracle_nufft3_2d(const double *x_in, const double *y_in, const double *f, long len_in, const double *s_in,
+                     const double *t_in, long len_out, double eps, double R, double *F, long *info) {
+    double Max_x = minmax_d(x_in, len_in, 1), min_x = minmax_d(x_in, len_in, 0);
+    double xb = (Max_x + min_x) / 2, X1 = fabs(Max_x - xb);
+    double Max_y = minmax_d(y_in, len_in, 1), min_y = minmax_d(y_in, len_in, 0);
+    double yb = (Max_y + min_y) / 2, Y1 = fabs(Max_y - yb);
+    double Max_s = minmax_d(s_in, len_out, 1), min_s = minmax_d(s_in, len_out, 0);
+    double sb = (Max_s + min_s) / 2, S = fabs(Max_s - sb);
+    double Max_t = minmax_d(t_in, len_out, 1), min_t = minmax_d(t_in, len_out, 0);
+    double tb = (Max_t + min_t) / 2, T = fabs(Max_t - tb);
+    if (!(X1 > 0) || !(Y1 > 0)) return -1;
+    double msp = 2 + 2 * (R * R) * (-log(eps / 76)) / (OR_PI * (R * R - 2)); /* :235 */
+    const long Mrx = 2 * (long)ceil((X1 * S / OR_PI) * R * R + R * msp);  /* :237-238 */
+    const long Mry = 2 * (long)ceil((Y1 * T / OR_PI) * R * R + R * msp);
+    const double Dx = 2 * OR_PI / (double)Mrx, Ds = 1, Dy = 2 * OR_PI / (double)Mry, Dt = 1; /* :240-241 */
+    const double kk_x = X1 / (OR_PI / 2), kk_y = Y1 / (OR_PI / 2);                            /* :243 */
+    double *x = (double *)malloc(sizeof(double) * (size_t)len_in), *y = (double *)malloc(sizeof(double) * (size_t)len_in);
+    double *s = (double *)malloc(sizeof(double) * (size_t)len_out), *t = (double *)malloc(sizeof(double) * (size_t)len_out);
+    for (long i = 0; i < len_in; ++i) { x[i] = x_in[i] / kk_x; y[i] = y_in[i] / kk_y; }      /* :245-246 */
+    for (long i = 0; i < len_out; ++i) { s[i] = s_in[i] * kk_x; t[i] = t_in[i] * kk_y; }     /* :247-248 */
+    Max_x = Max_x / kk_x; min_x = min_x / kk_x; xb = (Max_x + min_x) / 2;                     /* :250-264 */
+    Max_s = Max_s * kk_x; min_s = min_s * kk_x; sb = (Max_s + min_s) / 2;
+    Max_y = Max_y / kk_y; min_y = min_y / kk_y; yb = (Max_y + min_y) / 2;
+    Max_t = Max_t * kk_y; min_t = min_t * kk_y; tb = (Max_t + min_t) / 2;
+    const double b = (msp - 2) / (4 * OR_PI), t1 = 1 / (4 * b);                                /* :267 */
+    const int ms = (int)floor(msp - 2);
+    if (info) { info[0] = Mrx; info[1] = Mry; info[2] = ms; }
+
+    /* STEP 1 (:38-85): pre-phase, Gaussian spread with pre-compensation */
+    cplx *ft = (cplx *)calloc((size_t)(Mrx * Mry), sizeof(cplx));
+    const cplx *fc = (const cplx *)f;
+    const double fact0 = 1. / (4. * OR_PI * b), fact = fact0 * fact0;
+    for (long kk = 0; kk < len_in; ++kk) { /* serial: the sum order is fixed */
+        const double arg = sb * x[kk] + tb * y[kk];
+        const double re = fc[kk].re * cos(arg) + fc[kk].im * sin(arg);
+        const double im = fc[kk].im * cos(arg) - fc[kk].re * sin(arg);
+        const double x_temp = (x[kk] - xb) / Dx, y_temp = (y[kk] - yb) / Dy;
+        const long nn_offset = (long)floor(Mrx / 2 + x_temp), mm_offset = (long)floor(Mry / 2 + y_temp);
+        for (int mm = -ms; mm <= ms; ++mm) {
+            const long j = mm + mm_offset;
+            const double d_n_sj = (double)(j - Mry / 2);
+            for (int nn = -ms; nn <= ms; ++nn) {
+                const long i = nn + nn_offset;
+                const double d_n_si = (double)(i - Mrx / 2);
+                const double e = fact * exp(b * (Dy * Dy * d_n_sj * d_n_sj + Dx * Dx * d_n_si * d_n_si) -
+                                            t1 * ((x_temp - d_n_si) * (x_temp - d_n_si) + (y_temp - d_n_sj) * (y_temp - d_n_sj)));
+                ft[j * Mrx + i].re += re * e;
+                ft[j * Mrx + i].im += im * e;
+            }
+        }
+    }
+    /* STEP 2 (:283-292): forward 2D FFT of the Mry x Mrx grid */
+    oracle_fft2d((double *)ft, Mry, Mrx, -1);
+    /* shifts (:135-151): out[(j + Mry/2) % Mry][(i + Mrx/2) % Mrx] = (-1)^(i+j) in[j][i] */
+    cplx *Fs = (cplx *)malloc(sizeof(cplx) * (size_t)(Mrx * Mry));
+    for (long i = 0; i < Mrx; ++i)
+        for (long j = 0; j < Mry; ++j) {
+            const long ii = (i + Mrx / 2) % Mrx, jj = (j + Mry / 2) % Mry;
+            const double sg = ((i + j) & 1) ? -1.0 : 1.0;
+            Fs[jj * Mrx + ii].re = sg * ft[j * Mrx + i].re;
+            Fs[jj * Mrx + ii].im = sg * ft[j * Mrx + i].im;
+        }
+    /* STEP 3 (:156-194): Gaussian gather and post-compensation */
+    cplx *o = (cplx *)F;
+#pragma omp parallel for schedule(static)
+    for (long kk = 0; kk < len_out; ++kk) {
+        const long nsn = (long)floor(Mrx / 2 + (s[kk] - sb) / Ds);
+        const double difs = (Mrx / 2 + (s[kk] - sb) / Ds) - nsn;
+        const long ntn = (long)floor(Mry / 2 + (t[kk] - tb) / Dt);
+        const double dift = (Mry / 2 + (t[kk] - tb) / Dt) - ntn;
+        double a0 = 0, a1 = 0;
+        double tmp1 = Dy * (t[kk] - tb); tmp1 = tmp1 * tmp1;
+        double tmp2 = Dx * (s[kk] - sb); tmp2 = tmp2 * tmp2;
+        const double comp = exp(b * (tmp1 + tmp2));
+        for (long nn = nsn - ms; nn <= nsn + ms; ++nn)
+            for (long mm = ntn - ms; mm <= ntn + ms; ++mm) {
+                const double n_pi = (double)(mm - ntn), n_pj = (double)(nn - nsn);
+                const double e = exp(-t1 * ((dift - n_pi) * (dift - n_pi) + (difs - n_pj) * (difs - n_pj)));
+                a0 += Fs[mm * Mrx + nn].re * e;
+                a1 += Fs[mm * Mrx + nn].im * e;
+            }
+        const double arg = (s[kk] - sb) * xb + (t[kk] - tb) * yb;
+        o[kk].re = (a0 * cos(arg) + a1 * sin(arg)) * comp;
+        o[kk].im = (a1 * cos(arg) - a0 * sin(arg)) * comp;
+    }
+    free(ft); free(Fs); free(x); free(y); free(s); free(t);
+    return 0;
 }
 
 /* Literal NDFT2_2D.m:1-16, including its layout (output N x M, column-major

@@ -166,3 +166,18 @@ def test_oracle_ffbp_focuses_a_point_target(orc):
     data, sar = F.point_target_scene(Np=16, nf=64, Nx=32, R=2e3, step=0.08)
     with pytest.raises(ValueError):
         F.ffbp(data, sar, 1, 16)
+
+
+def test_oracle_nufft3_matches_exact_sum(orc):
+    """Restated NUFFT_2D_CPU (NFFT3_2D_C.cpp) against the exact type-3 sum at
+    the accuracies asked for."""
+    rng = np.random.default_rng(12)
+    M, N = 1500, 1200
+    x, y = rng.uniform(-3, 5, M), rng.uniform(-2, 2, M)
+    f = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    s, t = rng.uniform(-20, 10, N), rng.uniform(-15, 15, N)
+    exact = orc.ndft3_2d(x, y, f, s, t)
+    for eps in (1e-4, 1e-8, 1e-12):
+        F, info = orc.nufft3_2d(x, y, f, s, t, eps)
+        assert info["Mrx"] % 2 == 0 and info["Mry"] % 2 == 0
+        assert orc.rel_l2(F, exact) < max(eps, 1e-11)

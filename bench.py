@@ -161,18 +161,165 @@ def uneven_batch(seed: int = 4, count: int = 64):
                         "w": 6, "seed": seed})
 
 
-def pso_batch(seed: int = 6, count: int = 250, N: int = 44, M: int = 44 * 44):
-    """The PSO reflectarray synthesis shape: one transform per particle per
-    generation -- 250 particles (Synthesis/PSO/PSO.cu:27), a 44 x 44 element
-    array (kernel_single_v2.cu:30-31, M = 1936 points) onto the 2Nu x 2Nv =
-    44 x 44 spectral grid -- which the reference runs as one NFFT2_2D_GPU call
-    per particle (Synthesis.cu:395).  Points uniform, coefficients N(0,1)
-    complex; sigma 2, w 6."""
-    items = [dict(N=N, M=M) for _ in range(count)]
-    return dict(name=f"pso_batch_{count}x{N}x{N}_{M}", items=items, seed=seed, sigma=2.0, K=6,
-                config={"workload": "PSO far-field batch: one small transform per particle", "count": count,
-                        "N": [N, N], "points_per_transform": M, "points": count * M, "sigma": 2.0, "w": 6,
-                        "seed": seed})
+def pso_batch(seed: int = 6, count: int = 250):
+    """The reflectarray PSO synthesis' far-field step for one generation
+    (Synthesis/PSO/Synthesis.cu:385-405 for each of the 250 particles of
+    PSO.cu:27): 44 x 44 elements at 14.25 GHz (kernel_single_v2.cu:23-31),
+    spectral oversampling chi' = 4 (:72-80), so Nu = Nv = 44 and each far
+    field is 88 x 88; element positions on a 0.6-wavelength lattice with a
+    seeded +-0.05-wavelength jitter per particle (aperiodic arrays), unit
+    excitations with seeded phases, the visible-region filter.  One step =
+    the scaling, binning, reference-sign spread and filter for every
+    particle (positions change every generation, so the binning is in)."""
+    rng = np.random.default_rng(seed)
+    lam = 3e8 / 14.25e9
+    Mx = My = 44
+    aap = (Mx - 1) * (lam * 0.5 / 2.0)
+    a_prime = 4 * aap
+    beta = 2 * math.pi / lam
+    Nu = int((beta / 2) / (math.pi / a_prime)) + 1
+    Nv = int((beta / 2) / (math.pi / a_prime)) + 1
+    a_prime_f = float(np.float32(a_prime))
+    f32 = np.float32
+    sx = float(f32(float(f32(2 * Nu * (math.pi / a_prime_f))) / (2.0 * math.pi)))
+    sy = float(f32(float(f32(2 * Nv * (math.pi / a_prime_f))) / (2.0 * math.pi)))
+    gx, gy = np.meshgrid((np.arange(Mx) - (Mx - 1) / 2) * 0.6 * lam, (np.arange(My) - (My - 1) / 2) * 0.6 * lam)
+    X = [(gx + rng.uniform(-0.05, 0.05, gx.shape) * lam).ravel().astype(np.float32) for _ in range(count)]
+    Y = [(gy + rng.uniform(-0.05, 0.05, gy.shape) * lam).ravel().astype(np.float32) for _ in range(count)]
+    E = [np.exp(1j * rng.uniform(-math.pi, math.pi, gx.size)).astype(np.complex64) for _ in range(count)]
+    u = np.arange(-Nu, Nu) * (math.pi / a_prime)
+    v = np.arange(-Nv, Nv) * (math.pi / a_prime)
+    V, U = np.meshgrid(v, u, indexing="ij")
+    filt = (U * U + V * V <= beta * beta).astype(np.float32)
+    return dict(name=f"pso_far_field_{count}x{2 * Nv}x{2 * Nu}_{Mx * My}", X=X, Y=Y, E=E, Nu=Nu, Nv=Nv, sx=sx, sy=sy,
+                filter=filt, count=count, M=Mx * My,
+                config={"workload": "PSO reflectarray far field, one generation (scaling + binning + NFFT2_2D_GPU "
+                                    "sign + filter per particle)", "particles": count, "far_field": [2 * Nv, 2 * Nu],
+                        "elements": [Mx, My], "points": count * Mx * My, "sigma": 2.0, "w": 6, "seed": seed})
+
+
+def run_pso(args, wl):
+    """One generation's far fields: the batched step (nfft2d_batch_far_field)
+    vs one plan per particle (set_points + spread_ref + filter, the shape of
+    the reference's per-particle loop, through the library)."""
+    import torch
+
+    from miscellaneous_gb300.nfft import Batch, Plan
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    n1, n2, P, M = 2 * wl["Nv"], 2 * wl["Nu"], wl["count"], wl["M"]
+    X = [torch.from_numpy(a).to(dev) for a in wl["X"]]
+    Y = [torch.from_numpy(a).to(dev) for a in wl["Y"]]
+    E = [torch.from_numpy(a).to(dev) for a in wl["E"]]
+    filt = torch.from_numpy(wl["filter"].ravel()).to(dev)
+    outs = [torch.empty(n1 * n2, dtype=torch.complex64, device=dev) for _ in range(P)]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    batch = Batch([(n1, n2)] * P, sigma=2.0, K=6, stream=stream)
+
+    def batched():
+        batch.far_field(X, Y, E, wl["sx"], wl["sy"], filt, outs)
+
+    plans = [Plan(n1, n2, sigma=2.0, K=6, stream=stream) for _ in range(P)]
+    xs = [torch.empty(M, dtype=torch.float32, device=dev) for _ in range(P)]
+    ys = [torch.empty(M, dtype=torch.float32, device=dev) for _ in range(P)]
+
+    def sequential():
+        for p in range(P):
+            torch.mul(X[p], wl["sx"], out=xs[p])
+            torch.mul(Y[p], wl["sy"], out=ys[p])
+            plans[p].set_points(xs[p], ys[p], units="grid")
+            plans[p].spread_ref(E[p], out=outs[p])
+            outs[p].mul_(filt)
+
+    def timed(step):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            ev0.record(stream)
+            step()
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        return statistics.median(ms)
+
+    with ClockSampler(0) as clocks:
+        t_batch = timed(batched)
+    t_seq = timed(sequential)
+    batched()
+    batch.synchronize()
+    # accuracy: a few particles against the exact FP64 type-1 sum at the FP32-scaled points
+    errs = []
+    for p in (0, P // 2, P - 1):
+        x1 = (X[p] * wl["sx"]).double() / n1
+        x2 = (Y[p] * wl["sy"]).double() / n2
+        ref = ndft_type1(E[p], x1, x2, n1, n2, -1, torch) * filt.reshape(n1, n2)
+        errs.append(rel_l2(outs[p], ref, torch))
+    total = P * M
+    line = {"metric": METRIC, "value": total / (t_batch * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_batch, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": wl["config"],
+            "sequential_ms_per_step": t_seq, "batched_speedup": t_seq / t_batch,
+            "sequential": "one library plan per particle: set_points + spread_ref + filter, as the reference's loop",
+            "batched": "nfft2d_batch_far_field: FP32 scaling, binning, reference-sign spread and filter for all "
+                       "particles",
+            "accuracy": {"rel_l2_max": max(errs), "particles_checked": 3,
+                         "oracle": "exact FP64 type-1 sum at the FP32-scaled points, times the filter"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+    for p in plans:
+        p.close()
+    batch.close()
+
+
+def run_pso_reference(args, wl):
+    """The reference's own far-field loop on the GPU: one NFFT2_2D_GPU call
+    (NFFT/NFFT2_2D.cu compiled unchanged into oracle/_ref, dynamic-parallelism
+    interpolation) per particle, with the FP32 scaling and the filter around
+    it, for the same generation."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import torch
+
+    from oracle import ref_gpu
+    if not torch.cuda.is_available() or not ref_gpu.available():
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's NFFT2_2D_GPU needs a GPU and "
+                                                              "oracle/_ref/nfft2_2d_ref.cubin"}))
+        return
+    dev = torch.device("cuda", 0)
+    n1, n2, P, M = 2 * wl["Nv"], 2 * wl["Nu"], wl["count"], wl["M"]
+    X = [torch.from_numpy(a).to(dev) for a in wl["X"]]
+    Y = [torch.from_numpy(a).to(dev) for a in wl["Y"]]
+    E = [torch.from_numpy(a).to(dev) for a in wl["E"]]
+    filt = torch.from_numpy(wl["filter"]).to(dev)
+    steps = min(args.steps, 3)
+
+    def generation():
+        for p in range(P):
+            ff = ref_gpu.nfft2_2d_gpu(E[p], X[p] * wl["sx"], Y[p] * wl["sy"], n1, n2)
+            ff.mul_(filt)
+        torch.cuda.synchronize()
+
+    generation()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        generation()
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    value = P * M / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": wl["config"],
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 0, "kind": "reference",
+                             "sample": "the whole generation; the reference's own GPU code (NFFT/NFFT2_2D.cu, "
+                                       "oracle/_ref) once per particle -- the reference has no CPU path for this "
+                                       "step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def ffbp_scene(seed: int = 7, Np: int = 64, nf: int = 216, Nx: int = 128, step: float = 0.08, R: float = 10e3):
@@ -1395,9 +1542,14 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the least-squares workload has no reference counterpart"}))
             return
         run_lsq(args, wl)
-    elif args.workload in ("batch", "pso"):
+    elif args.workload == "pso":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batch workloads have no reference counterpart"}))
+            run_pso_reference(args, wl)
+        else:
+            run_pso(args, wl)
+    elif args.workload == "batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no reference counterpart"}))
             return
         run_batch(args, wl)
     elif args.impl == "reference":

@@ -255,6 +255,23 @@ int nfft2d_batch_adjoint(nfft2d_batch batch, const void *const *f, void *const *
  * PSO synthesis (Synthesis/PSO/Synthesis.cu:395) done for all particles at
  * once. */
 int nfft2d_batch_spread_ref(nfft2d_batch batch, const void *const *f, void *const *F);
+/* The far-field step of the reflectarray PSO synthesis for every particle of
+ * the batch at once (Synthesis/PSO/Synthesis.cu:385-405, raFarFieldCalculation
+ * around its NFFT2_2D_GPU call; the reference runs it once per particle,
+ * PSO.cu:348): per transform t,
+ *   X' = X[t] * scale_x,  Y' = Y[t] * scale_y        (FP32, :388-389; the
+ *        reference's scales are 2 Nu (pi / a') / (2 pi) and 2 Nv (pi / b') / (2 pi))
+ *   far_field[t] = type 1, sign -1, at (X', Y')      (NFFT2_2D_GPU, :395)
+ *   far_field[t] .*= filter                          (farFieldFiltering, :402)
+ * M points per transform; X, Y: host arrays of `count` device pointers to M
+ * floats; excitations: count device pointers to M float2; filter: DEVICE,
+ * N1 N2 floats (NULL: none; every transform must then have the same size);
+ * far_field: count device pointers to N1 N2 float2.  Binds the points
+ * (synchronizes, as nfft2d_batch_set_points), then runs asynchronously on
+ * the batch's stream. */
+int nfft2d_batch_far_field(nfft2d_batch batch, long long M, const float *const *X, const float *const *Y,
+                           float scale_x, float scale_y, const void *const *excitations, const float *filter,
+                           void *const *far_field);
 int nfft2d_batch_set_graph(nfft2d_batch batch, int on);
 /* Waits for the batch's work and reports a latched device-side error once
  * (cleared after it is read), as nfft2d_synchronize does for plans. */

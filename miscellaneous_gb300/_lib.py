@@ -136,6 +136,7 @@ _SIGNATURES = {
     "nfft2d_batch_adjoint": (_I, [_P, _P, _P]),
     "nfft2d_batch_spread_ref": (_I, [_P, _P, _P]),
     "nfft2d_batch_set_graph": (_I, [_P, _I]),
+    "nfft2d_batch_far_field": (_I, [_P, _LL, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P]),
     "nfft2d_batch_synchronize": (_I, [_P]),
     "nfft2d_batch_selftest_wait_timeout": (_I, [_P, _I]),
     "nfft2d_knab_window": (_I, [_D, _D, _I, _I, _P, _I, ctypes.POINTER(_I)]),

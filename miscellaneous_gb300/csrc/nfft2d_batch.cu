@@ -492,6 +492,30 @@ int run(nfft2d_batch_s *b, int type, const void *const *in, void *const *out) {
 
 }  // namespace
 
+// Far-field step of the reflectarray PSO synthesis, for every particle of a
+// batch: the FP32 coordinate scaling of Synthesis/PSO/Synthesis.cu:388-389,
+// the reference-sign spread of :395 and the filter of :402.
+namespace {
+__global__ void k_scale_points(const float *const *__restrict__ X, const float *const *__restrict__ Y, long long M,
+                               float sx, float sy, float *__restrict__ xs, float *__restrict__ ys) {
+    const int t = blockIdx.y;
+    const float *x = X[t], *y = Y[t];
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < M;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        xs[t * M + i] = x[i] * sx;  // vectorMulConstant<float>
+        ys[t * M + i] = y[i] * sy;
+    }
+}
+__global__ void k_filter(float2 *const *__restrict__ F, const float *__restrict__ filt, long long n) {
+    float2 *f = F[blockIdx.y];
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const float w = filt[i];
+        f[i] = make_float2(w * f[i].x, w * f[i].y);  // farFieldFiltering
+    }
+}
+}  // namespace
+
 extern "C" {
 
 int nfft2d_batch_create_k(nfft2d_batch *out, int count, const int *N1, const int *N2, const int *K, double sigma,
@@ -660,6 +684,73 @@ int nfft2d_batch_forward(nfft2d_batch b, const void *const *F, void *const *f) {
 int nfft2d_batch_adjoint(nfft2d_batch b, const void *const *f, void *const *F) { return run(b, 1, f, F); }
 
 int nfft2d_batch_spread_ref(nfft2d_batch b, const void *const *f, void *const *F) { return run(b, -1, f, F); }
+
+int nfft2d_batch_far_field(nfft2d_batch b, long long M, const float *const *X, const float *const *Y, float scale_x,
+                           float scale_y, const void *const *excitations, const float *filter,
+                           void *const *far_field) {
+    if (!b || !X || !Y || !excitations || !far_field || M < 0 || M > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;
+    const int n = b->count;
+    long long cells = -1;
+    for (int i = 0; i < n; ++i) {
+        const long long c = static_cast<long long>(b->plans[i]->N1) * b->plans[i]->N2;
+        if (cells >= 0 && c != cells && filter) return NFFT2D_ERR_INVALID_ARG;  // one filter for one grid size
+        cells = c;
+        if (M > 0 && (!X[i] || !Y[i])) return NFFT2D_ERR_INVALID_ARG;
+    }
+    // the caller's coordinates were written on its stream
+    B_TRY(cudaEventRecord(b->ev_in, b->user_stream));
+    B_TRY(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
+    float *xs = nullptr, *ys = nullptr;
+    const float **dxy = nullptr;
+    const size_t pts = static_cast<size_t>(n) * static_cast<size_t>(M);
+    B_TRY(cudaMallocAsync(&xs, sizeof(float) * pts + 16, b->stream));
+    B_TRY(cudaMallocAsync(&ys, sizeof(float) * pts + 16, b->stream));
+    B_TRY(cudaMallocAsync(&dxy, sizeof(float *) * 2 * n, b->stream));
+    std::vector<const float *> hxy(2 * static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) {
+        hxy[i] = X[i];
+        hxy[n + i] = Y[i];
+    }
+    int st = NFFT2D_OK;
+    if (cudaMemcpyAsync(dxy, hxy.data(), sizeof(float *) * 2 * n, cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
+        st = NFFT2D_ERR_CUDA;
+    if (st == NFFT2D_OK && M > 0) {
+        const dim3 grid(static_cast<unsigned>(std::min<long long>((M + 255) / 256, 64)), static_cast<unsigned>(n));
+        k_scale_points<<<grid, 256, 0, b->stream>>>(dxy, dxy + n, M, scale_x, scale_y, xs, ys);
+        if (cudaGetLastError() != cudaSuccess) st = NFFT2D_ERR_CUDA;
+    }
+    if (st == NFFT2D_OK) {
+        std::vector<long long> Ms(static_cast<size_t>(n), M);
+        std::vector<const void *> px(static_cast<size_t>(n)), py(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) {
+            px[i] = xs + static_cast<size_t>(i) * M;
+            py[i] = ys + static_cast<size_t>(i) * M;
+        }
+        st = nfft2d_batch_set_points(b, Ms.data(), px.data(), py.data(), NFFT2D_COORD_F32, NFFT2D_UNITS_GRID);
+    }
+    cudaFreeAsync(xs, b->stream);
+    cudaFreeAsync(ys, b->stream);
+    cudaFreeAsync(dxy, b->stream);
+    if (st != NFFT2D_OK) return st;
+    if ((st = run(b, -1, excitations, far_field)) != NFFT2D_OK) return st;  // NFFT2_2D_GPU for every particle
+    if (filter && cells > 0) {
+        float2 **dF = nullptr;
+        B_TRY(cudaMallocAsync(&dF, sizeof(float2 *) * n, b->user_stream));
+        std::vector<float2 *> hF(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) hF[i] = static_cast<float2 *>(far_field[i]);
+        const cudaError_t e = cudaMemcpyAsync(dF, hF.data(), sizeof(float2 *) * n, cudaMemcpyHostToDevice,
+                                              b->user_stream);
+        if (e == cudaSuccess) {
+            const dim3 grid(static_cast<unsigned>(std::min<long long>((cells + 255) / 256, 64)),
+                            static_cast<unsigned>(n));
+            k_filter<<<grid, 256, 0, b->user_stream>>>(dF, filter, cells);
+        }
+        cudaFreeAsync(dF, b->user_stream);
+        B_TRY(e);
+        B_TRY(cudaGetLastError());
+    }
+    return NFFT2D_OK;
+}
 
 int nfft2d_batch_set_graph(nfft2d_batch b, int on) {
     if (!b) return NFFT2D_ERR_INVALID_ARG;

@@ -290,8 +290,54 @@ class Batch:
         check(self._lib.nfft2d_batch_spread_ref(self._h, self._ptrs(fs), self._ptrs(outs)), "nfft2d_batch_spread_ref")
         return outs
 
+    def far_field(self, X, Y, excitations, scale_x: float, scale_y: float, filter: torch.Tensor | None = None,
+                  outs=None):
+        """The PSO far-field step for every particle (nfft2d_batch_far_field,
+        Synthesis/PSO/Synthesis.cu:385-405): element positions X[t], Y[t]
+        (float32, one tensor per particle, equal lengths), excitations[t]
+        (complex64), the FP32 scales of :388-389 (see pso_far_field_scales)
+        and the spectral filter (float32, N1*N2).  Returns the far fields."""
+        if len(X) != self.count or len(Y) != self.count or len(excitations) != self.count:
+            raise ValueError("one X, Y and excitation per transform")
+        M = X[0].numel()
+        for a, b, e in zip(X, Y, excitations):
+            _require_cuda(a, "X", torch.float32, M)
+            _require_cuda(b, "Y", torch.float32, M)
+            _require_cuda(e, "excitations", torch.complex64, M)
+        if filter is not None:
+            n1, n2 = self.sizes[0]
+            _require_cuda(filter, "filter", torch.float32, n1 * n2)
+        if outs is None:
+            outs = [torch.empty(n1 * n2, dtype=torch.complex64, device=X[0].device) for n1, n2 in self.sizes]
+        check(self._lib.nfft2d_batch_far_field(self._h, M, self._ptrs(X), self._ptrs(Y), float(scale_x),
+                                               float(scale_y), self._ptrs(excitations),
+                                               _ptr(filter), self._ptrs(outs)), "nfft2d_batch_far_field")
+        self.M = [M] * self.count
+        self._keep = (list(X), list(Y))
+        return outs
+
     def synchronize(self) -> None:
         check(self._lib.nfft2d_batch_synchronize(self._h), "nfft2d_batch_synchronize")
+
+
+def pso_spectral_grid(u_max: float, v_max: float, a_prime: float, b_prime: float):
+    """Nu, Nv of the PSO synthesis' spectral grid (Synthesis/PSO/Synthesis.cu:82-83):
+    Nu = (int)(u_max / (pi / a')) + 1; the far field is 2 Nv x 2 Nu."""
+    import math
+    return int(u_max / (math.pi / a_prime)) + 1, int(v_max / (math.pi / b_prime)) + 1
+
+
+def pso_far_field_scales(Nu: int, Nv: int, a_prime_f: float, b_prime_f: float):
+    """The FP32 coordinate scales of Synthesis.cu:388-389,
+    float(2 Nu (pi / a')) / (float(2) pi), rounded to FP32 as the reference
+    passes them to vectorMulConstant<float>."""
+    import math
+
+    import numpy as np
+    f32 = np.float32
+    sx = float(f32(2 * Nu * (math.pi / float(f32(a_prime_f))))) / (2.0 * math.pi)
+    sy = float(f32(2 * Nv * (math.pi / float(f32(b_prime_f))))) / (2.0 * math.pi)
+    return float(f32(sx)), float(f32(sy))
 
 
 # ---------------------------------------------------------------------------

@@ -775,10 +775,17 @@ def run_ours(args, wl):
     import torch.distributed as dist
 
     from miscellaneous_gb300.nfft import Plan
+    from miscellaneous_gb300.shard import ShardedPlan
 
     world, rank, local = dist_env()
     if world > 1:
         dist.init_process_group("nccl")
+        # one transform of world * M points: each rank draws its own M points
+        # (the workload's distribution, a rank-specific seed) and keeps them
+        if wl["name"].startswith("clustered"):
+            wl = clustered_config3(seed=3 + 1000 * rank, K=wl["K"])
+        elif wl["name"].startswith("polar"):
+            wl = polar_raster(seed=2 + 1000 * rank, K=wl["K"])
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
@@ -791,7 +798,8 @@ def run_ours(args, wl):
     f = torch.from_numpy(wl["f"]).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    plan = Plan(N1, N2, sigma=wl["sigma"], K=wl["K"], precision="f32", stream=stream)
+    sharded = ShardedPlan(N1, N2, sigma=wl["sigma"], K=wl["K"], precision="f32", stream=stream)
+    plan = sharded.plan
     if args.fft_mode != "auto":
         plan.set_tuning(fft_mode={"cufft": 0, "pruned": 1, "fused": 2}[args.fft_mode])
     plan.set_points(x1, x2, units="unit")
@@ -807,8 +815,8 @@ def run_ours(args, wl):
     F_out = torch.empty(N1 * N2, dtype=torch.complex64, device=dev)
 
     def step():
-        plan.forward(F, out=f_out)
-        plan.adjoint(f, out=F_out)
+        sharded.forward(F, out=f_out)  # this rank's points, no collective
+        sharded.adjoint(f, out=F_out)  # this rank's points, then the sum all-reduce (N > 1)
 
     # the timed steps run without the plan's per-stage events (recording them
     # costs ~10 % of a polar step); the stage breakdown comes from as many
@@ -905,9 +913,9 @@ def run_ours(args, wl):
                 ev_in.record(cs)
             plan.set_points(dx1, dx2, units="unit", sync=False)
             stream.wait_event(ev_in)
-            plan.forward(dF, out=f_out)
+            sharded.forward(dF, out=f_out)
             ev_fwd.record(stream)
-            plan.adjoint(df, out=F_out)
+            sharded.adjoint(df, out=F_out)
             cs.wait_event(ev_fwd)
             with torch.cuda.stream(cs):
                 hf_out.copy_(f_out, non_blocking=True)
@@ -989,7 +997,7 @@ def run_ours(args, wl):
                          "kernels; the line's own FFT is the fused passes"}
 
     study = None
-    if wl["name"].startswith("clustered") and not args.no_precision_study:
+    if wl["name"].startswith("clustered") and not args.no_precision_study and world == 1:
         study = precision_study(args, wl, [k for k in (4, 6, 8) if k != wl["K"]], x1, x2, F, f, stream, flush,
                                 torch)
         study[f"w{wl['K']}"] = {"ms_per_step": t_step, "value": M / (t_step * 1e-3), "unit": UNIT}
@@ -1013,7 +1021,10 @@ def run_ours(args, wl):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(wl["config"], l2="256 MB buffer written between timed steps (working set %s L2)"
                            % ("<" if 8 * G + 36 * M < L2_BYTES else ">"),
-                           points_prebinned=True, parallelism="replicas" if world > 1 else "single GPU",
+                           points_prebinned=True,
+                           parallelism=("points sharded: one transform of %d x M points, each rank gathers and "
+                                        "spreads its own M, NCCL sum all-reduce of the N1 x N2 adjoint" % world)
+                           if world > 1 else "single GPU",
                            tuning=(tuned or {}).get("tuning"), plan=plan.info()),
             "stages_ms": stage,
             "stages_note": STAGES_NOTE[fused],
@@ -1370,6 +1381,39 @@ def run_batch(args, wl):
 
     t_seq = timed(sequential)
     batch.synchronize()
+    # what the sequential arm is made of: each transform's kernel time (its
+    # plan's stage events) against the arm's wall time; the difference is
+    # the launch gaps that batching can remove
+    for p in plans:
+        p.enable_timing(True)
+    per = []
+    for _ in range(3):
+        for i, (p, F, fo) in enumerate(zip(plans, Fs, f_out)):
+            p.forward(F, out=fo)
+            p.synchronize()
+            tf = p.timings()
+            p.adjoint(fs[i], out=F_out[i])
+            p.synchronize()
+            ta = p.timings()
+            k = (tf["pad_ms"] + tf["fft_type2_ms"] + tf["halo_fill_ms"] + tf["gather_ms"] + ta["spread_ms"]
+                 + ta["fold_ms"] + ta["fft_type1_ms"] + ta["crop_ms"])
+            if len(per) <= i:
+                per.append([])
+            per[i].append(k)
+    for p in plans:
+        p.enable_timing(False)
+    kern = [statistics.median(v) for v in per]
+    table = {}
+    for (n1, _), it, k in zip(sizes, wl["items"], kern):
+        row = table.setdefault(str(n1), {"transforms": 0, "points": 0, "kernel_ms": 0.0})
+        row["transforms"] += 1
+        row["points"] += it["M"]
+        row["kernel_ms"] += k
+    breakdown = {"kernel_ms_sum": sum(kern), "sequential_wall_ms": t_seq,
+                 "launch_gap_share": max(0.0, 1.0 - sum(kern) / t_seq),
+                 "batched_over_kernel_sum": t_batch / sum(kern), "by_grid_size": table,
+                 "note": "kernel_ms = the transform's stage events (pad, FFTs, fill, gather, spread, fold, crop) "
+                         "timed one transform at a time; batching can remove at most the launch gaps"}
     accuracy = None
     if not args.no_accuracy:
         # the batched results themselves: forward on point subsets of a few
@@ -1400,6 +1444,7 @@ def run_batch(args, wl):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(wl["config"], l2="256 MB buffer written between timed steps"),
             "sequential_ms_per_step": t_seq, "batched_speedup": t_seq / t_batch,
+            "sequential_breakdown": breakdown,
             "sequential": "one forward + one adjoint per transform through pre-created single-transform plans",
             "batched": "nfft2d_batch_forward + nfft2d_batch_adjoint, stage sequence replayed as a CUDA graph",
             "accuracy": accuracy}

@@ -46,3 +46,44 @@ def sharded_adjoint(local_type1: Callable[[torch.Tensor], torch.Tensor], f_local
 def shard_batch(n_transforms: int, rank: int, world: int) -> list[int]:
     """Round-robin assignment of independent transforms to ranks."""
     return list(range(rank, n_transforms, world))
+
+
+class ShardedPlan:
+    """One 2D NFFT whose nonuniform points are split over the ranks of a
+    process group, one GPU per rank: each rank holds a library plan of the
+    full N1 x N2 problem bound to its own points.
+
+    forward(F): every rank gathers its points from the same coefficients
+    (outputs stay sharded; no collective).  adjoint(f_local): every rank
+    spreads, transforms and crops its points, then one sum all-reduce of
+    the N1 x N2 result (NCCL on GPUs) gives every rank the full adjoint.
+    """
+
+    def __init__(self, N1: int, N2: int, sigma: float = 2.0, K: int = 6, precision: str = "f32",
+                 stream: torch.cuda.Stream | None = None, group=None):
+        from .nfft import Plan
+        self.plan = Plan(N1, N2, sigma=sigma, K=K, precision=precision, stream=stream)
+        self.group = group
+        self.world = dist.get_world_size(group) if dist.is_available() and dist.is_initialized() else 1
+        self.rank = dist.get_rank(group) if self.world > 1 else 0
+
+    def set_points(self, x1: torch.Tensor, x2: torch.Tensor, units: str = "unit", full: bool = False,
+                   sync: bool = True) -> None:
+        """Bind this rank's points: x1, x2 are its own slice, or (full=True)
+        the whole point set, of which the rank keeps shard_bounds' slice."""
+        if full:
+            s, e = shard_bounds(x1.numel(), self.rank, self.world)
+            x1, x2 = x1[s:e].contiguous(), x2[s:e].contiguous()
+        self.plan.set_points(x1, x2, units=units, sync=sync)
+
+    def forward(self, F: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        return sharded_forward(lambda c: self.plan.forward(c, out=out), F)
+
+    def adjoint(self, f_local: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        return sharded_adjoint(lambda v: self.plan.adjoint(v, out=out), f_local, self.group)
+
+    def synchronize(self) -> None:
+        self.plan.synchronize()
+
+    def close(self) -> None:
+        self.plan.close()

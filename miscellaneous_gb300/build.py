@@ -1,4 +1,4 @@
-"""Build recipe for libnfft2d_gb300.so (sm_103a) and its C++ compat driver.
+"""Build recipe for libnfft2d_gb300.so (sm_103a).
 
 Each CUDA translation unit is compiled by nvcc in parallel, then linked into
 one shared library in ``miscellaneous_gb300/lib``.  Objects are rebuilt only
@@ -93,31 +93,6 @@ def build(verbose_ptxas: bool = False, jobs: int | None = None) -> str:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
-
-
-COMPAT_DRIVER_SRC = os.path.join(PKG, "csrc", "tools", "compat_driver.cpp")
-COMPAT_DRIVER_BIN = os.path.join(LIB_DIR, "nfft2d_compat_driver")
-
-
-def build_compat_driver() -> str:
-    """Build the C++ program that calls the reference signatures
-    (NFFT2_2D_GPU / NDFT2_2D_GPU overloads from include/NFFT2_2D.cuh and
-    include/NDFT2_2D.cuh) exactly as a reference caller would, linked against
-    libnfft2d_gb300.so."""
-    lib = build()
-    if not _stale(COMPAT_DRIVER_BIN, [COMPAT_DRIVER_SRC, lib] + _headers()):
-        return COMPAT_DRIVER_BIN
-    lib64 = os.path.join(cuda_home(), "lib64")
-    inc = os.path.join(cuda_home(), "include")
-    tmp = COMPAT_DRIVER_BIN + f".tmp{os.getpid()}"
-    cmd = ["g++", "-O2", "-std=c++17", COMPAT_DRIVER_SRC, "-o", tmp, "-I", INCLUDE, "-I", inc,
-           "-L", LIB_DIR, "-lnfft2d_gb300", "-L", lib64, "-lcudart",
-           f"-Wl,-rpath,{LIB_DIR}", f"-Wl,-rpath,{lib64}"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"compat driver build failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, COMPAT_DRIVER_BIN)
-    return COMPAT_DRIVER_BIN
 
 
 if __name__ == "__main__":

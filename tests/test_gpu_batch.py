@@ -54,6 +54,9 @@ def test_batch_matches_single_plans(orc, graph):
                 assert orc.rel_l2(got_F, b) < 1e-6, (call, t)
                 g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
                 assert orc.rel_l2(got_f, orc.ndft_type2(F, g1, g2, sign=-1)) < 1e-5, (call, t)
+                # the batched adjoint against the exact FP64 type-1 sum itself
+                exact_F = orc.ndft_type1(f.astype(np.complex128), g1, g2, n1, n2, sign=+1)
+                assert orc.rel_l2(got_F.reshape(n1, n2), exact_F) < 1e-5, (call, t)
 
 
 def test_batch_rebinning_recaptures_the_graph(orc):
@@ -98,6 +101,13 @@ def test_pso_shaped_batch_matches_single_plans():
             r = p.spread_ref(torch.from_numpy(fs[t]).cuda()).reshape(-1).cpu().numpy()
         oR = outs_R[t].cpu().numpy().reshape(-1)
         assert np.linalg.norm(oR - r) / np.linalg.norm(r) < 1e-6
+        # the batched spread_ref and adjoint against the exact FP64 type-1 sums
+        g1, g2 = xs[t][0].astype(np.float64) * 44, xs[t][1].astype(np.float64) * 44
+        f64 = fs[t].astype(np.complex128)
+        ex_R = orc.ndft_type1(f64, g1, g2, 44, 44, sign=-1).reshape(-1)
+        ex_A = orc.ndft_type1(f64, g1, g2, 44, 44, sign=+1).reshape(-1)
+        assert np.linalg.norm(oR - ex_R) / np.linalg.norm(ex_R) < 1e-5
+        assert np.linalg.norm(oF - ex_A) / np.linalg.norm(ex_A) < 1e-5
     b.close()
 
 
@@ -127,3 +137,5 @@ def test_uneven_window_widths_in_one_batch(orc, graph):
             g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
             bar = 1e-5 if K >= 3 else 1e-3  # the window itself is off by 4e-4 at K = 2 (sigma = 2)
             assert orc.rel_l2(got_f, orc.ndft_type2(F, g1, g2, sign=-1)) < bar, t
+            exact_F = orc.ndft_type1(f.astype(np.complex128), g1, g2, n1, n2, sign=+1)
+            assert orc.rel_l2(got_F.reshape(n1, n2), exact_F) < bar, t

@@ -73,7 +73,7 @@ def test_batch_rebinning_recaptures_the_graph(orc):
                 assert orc.rel_l2(outs[t].cpu().numpy(), orc.ndft_type2(F, g1, g2, sign=-1)) < 1e-5
 
 
-def test_pso_shaped_batch_matches_single_plans():
+def test_pso_shaped_batch_matches_single_plans(orc):
     """The PSO synthesis shape: 250 transforms of 1936 points on a 44 x 44
     grid (a grid that is not a whole number of 16 x 16 tiles), replayed twice
     from the captured graph."""

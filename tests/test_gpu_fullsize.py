@@ -46,14 +46,15 @@ def _rel(a, b):
 @pytest.fixture(scope="module")
 def clustered():
     """Config 3: 2048^2 coefficients, 2^24 points from a wrapped 2D Gaussian
-    (sigma 0.15), generated on the GPU."""
-    g = torch.Generator(device=DEV).manual_seed(3)
+    (sigma 0.15): NumPy PCG64, seed 3, the benchmark's own inputs."""
+    rng = np.random.default_rng(3)
     M, N = 1 << 24, 2048
-    x1 = torch.remainder(torch.randn(M, device=DEV, generator=g) * 0.15 + 0.5, 1.0) - 0.5
-    x2 = torch.remainder(torch.randn(M, device=DEV, generator=g) * 0.15 + 0.5, 1.0) - 0.5
-    F = torch.randn(N, N, dtype=torch.complex64, device=DEV, generator=g)
-    f = torch.randn(M, dtype=torch.complex64, device=DEV, generator=g)
-    return x1.float().contiguous(), x2.float().contiguous(), F, f
+    x1 = np.mod(rng.normal(0.0, 0.15, M) + 0.5, 1.0) - 0.5
+    x2 = np.mod(rng.normal(0.0, 0.15, M) + 0.5, 1.0) - 0.5
+    F = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))).astype(np.complex64)
+    f = (rng.standard_normal(M) + 1j * rng.standard_normal(M)).astype(np.complex64)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+    return t(x1.astype(np.float32)), t(x2.astype(np.float32)), t(F), t(f)
 
 
 @pytest.mark.parametrize("K", [4, 6, 8])
@@ -66,7 +67,8 @@ def test_clustered_full_size(clustered, K):
         AF = p.forward(F.reshape(-1))
         AHf = p.adjoint(f).reshape(-1)
         p.synchronize()
-    idx = torch.randperm(x1.numel(), generator=torch.Generator().manual_seed(K))[:4096].to(DEV)
+    # the exact FP64 sum on a 65,536-point random subset (PCG64)
+    idx = torch.from_numpy(np.random.default_rng(100 + K).choice(x1.numel(), 65536, replace=False)).to(DEV)
     assert _rel(AF[idx], _ndft_subset(F, x1, x2, idx, -1)) < 1e-5
     lhs = torch.vdot(f.to(torch.complex128), AF.to(torch.complex128))
     rhs = torch.vdot(AHf.to(torch.complex128), F.reshape(-1).to(torch.complex128))

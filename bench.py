@@ -813,6 +813,8 @@ def run_ours(args, wl):
         tuned = autotune.tune(plan, x1, x2, F, f, use_cache=False)  # measured here, outside the timed region
     f_out = torch.empty(M, dtype=torch.complex64, device=dev)
     F_out = torch.empty(N1 * N2, dtype=torch.complex64, device=dev)
+    if args.io_order == "binned":  # profiling runs of the binned order (the line's own arm stays in caller order)
+        plan.set_tuning(io_order="binned")
 
     def step():
         sharded.forward(F, out=f_out)  # this rank's points, no collective
@@ -861,6 +863,7 @@ def run_ours(args, wl):
         stage["crop"] += t["crop_ms"]
         flush.zero_()
     plan.enable_timing(False)
+    plan.set_tuning(io_order="caller")  # the checks and e2e below use the caller's order
     t_step = sum(step_ms) / len(step_ms)
     if world > 1:
         tt = torch.tensor([t_step], device=dev)
@@ -1007,6 +1010,36 @@ def run_ours(args, wl):
                                         subset_points=accuracy["subset_points"])
         study = dict(sorted(study.items()))
 
+    # the same step with the per-point arrays in the plan's binned order (an
+    # iterative solver keeps its vectors in that order): the gather writes and
+    # the spread reads them contiguously instead of at random caller indices
+    binned = None
+    if world == 1:
+        perm = plan.permutation().long()
+        f_b = f[perm].contiguous()
+        plan.set_tuning(io_order="binned")
+        for _ in range(args.warmup):
+            plan.forward(F, out=f_out)
+            plan.adjoint(f_b, out=F_out)
+            flush.zero_()
+        torch.cuda.synchronize()
+        bms = []
+        for _ in range(args.steps):
+            ev0.record(stream)
+            plan.forward(F, out=f_out)
+            plan.adjoint(f_b, out=F_out)
+            ev1.record(stream)
+            ev1.synchronize()
+            bms.append(ev0.elapsed_time(ev1))
+            flush.zero_()
+        plan.set_tuning(io_order="caller")
+        tb = sum(bms) / len(bms)
+        binned = {"ms_per_step": tb, "value": M / (tb * 1e-3), "unit": UNIT,
+                  "traffic": {k: ncu_traffic(k + "_binned", wl["name"]) for k in ("k_gather_direct", "k_spread_tiled")},
+                  "note": "io_order binned (nfft2d_tuning): f in the plan's binned order, same points and grid; "
+                          "traffic = DRAM bytes per launch from the committed ncu summary"}
+        del f_b, perm
+
     small = spread_small_cases(stream) if rank == 0 and not args.no_reference_gpu else None
 
     cpu = None
@@ -1039,6 +1072,7 @@ def run_ours(args, wl):
                                         "note": "binning timed by the plan's events, plus one execute step"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
             "precision_study": study,
+            "binned_io": binned,
             "spread_small_cases": small,
             "gpu_launches": 6 * args.steps,
             "gpu_launches_note": ("our kernels in the timed region per step: column FFT+pad, row FFT+fill, gather, "
@@ -1562,6 +1596,8 @@ def main():
     ap.add_argument("--fft-mode", choices=["auto", "cufft", "pruned", "fused"], default="auto",
                     help="oversampled FFT: auto (fused passes below 2048^2 cells, else cuFFT), cuFFT 2D plan, "
                          "cuFFT passes, fused")
+    ap.add_argument("--io-order", choices=["caller", "binned"], default="caller",
+                    help="per-point arrays of the timed steps in the caller's or the plan's binned order")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
     ap.add_argument("--K", type=int, default=None,

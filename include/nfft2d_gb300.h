@@ -116,7 +116,21 @@ typedef struct {
                               halo fill, halo fold and crop (FP32 plans, grid
                               sides powers of two from 64 to 4096, else
                               NFFT2D_ERR_UNSUPPORTED)                           */
+    int io_order;          /* -1 = keep.  NFFT2D_ORDER_CALLER (initially): the
+                              per-point arrays (f of type 2 / type 1, v, g1,
+                              g2 of grad_x) follow the caller's point order.
+                              NFFT2D_ORDER_BINNED: they follow the plan's
+                              binned order instead -- entry i belongs to the
+                              caller's point perm[i] of nfft2d_get_permutation
+                              -- so the gather writes and the spread reads
+                              them contiguously (a caller that keeps its
+                              vectors in that order, an iterative solver, saves
+                              the random 8-byte accesses of the caller's
+                              order).  Set it before set_points or after. */
 } nfft2d_tuning;
+
+#define NFFT2D_ORDER_CALLER 0
+#define NFFT2D_ORDER_BINNED 1
 
 /* Stage times in milliseconds, from CUDA events recorded on the plan's
  * stream while timing is enabled.  Each field holds the most recent run of
@@ -147,6 +161,11 @@ int nfft2d_plan_destroy(nfft2d_plan plan);
 int nfft2d_set_stream(nfft2d_plan plan, void *stream);
 int nfft2d_set_tuning(nfft2d_plan plan, const nfft2d_tuning *tuning);
 int nfft2d_get_info(nfft2d_plan plan, nfft2d_info *info);
+
+/* The binned order of the points set last: perm[i] = the caller's index of
+ * the point at binned position i (M ints, DEVICE).  Asynchronous on the
+ * plan's stream.  No reference counterpart. */
+int nfft2d_get_permutation(nfft2d_plan plan, int *perm);
 
 /* Host-only: the layout a plan with these parameters would use (no GPU
  * needed).  tile = 0 picks the default. */

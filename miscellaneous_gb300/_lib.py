@@ -52,9 +52,14 @@ class Info(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+ORDER_CALLER = 0
+ORDER_BINNED = 1
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int), ("chunk", ctypes.c_int), ("gather_variant", ctypes.c_int),
-                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int), ("fft_mode", ctypes.c_int)]
+                ("spread_variant", ctypes.c_int), ("compensated", ctypes.c_int), ("fft_mode", ctypes.c_int),
+                ("io_order", ctypes.c_int)]
 
 
 class Timings(ctypes.Structure):
@@ -110,6 +115,7 @@ _SIGNATURES = {
     "nfft2d_set_stream": (_I, [_P, _P]),
     "nfft2d_set_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
     "nfft2d_get_info": (_I, [_P, ctypes.POINTER(Info)]),
+    "nfft2d_get_permutation": (_I, [_P, _P]),
     "nfft2d_layout_query": (_I, [_I, _I, _D, _I, _I, _I, ctypes.POINTER(Info)]),
     "nfft2d_set_points": (_I, [_P, _LL, _P, _P, _I, _I]),
     "nfft2d_set_points_async": (_I, [_P, _LL, _P, _P, _I, _I]),

@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
         ch.z = min(kSpreadItem, ch.z - first);
         const int tr = ch.x / D.g.tiles2, tc = ch.x - tr * D.g.tiles2;
         fs.map = &D.tmap;  // this transform's grid (strip-patch box)
-        spread_item<K>(D.recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, io[t].in, scr, fs, wp, status);
+        spread_item<K>(D.recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, io[t].in, 0, scr, fs, wp, status);
     }
     if (lane == 0) bulk_wait_all();
 }

@@ -110,8 +110,9 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                 latch_error(a.status, kErrBounds);
                 continue;
             }
+            const int io = a.binned_io ? ch.y + i : raw.w;  // caller's index or binned position
             if (MODE == 0) {
-                out[raw.w] = gather_point<K, COMP>(patch, PC, g.Ke, lr, lc, t1, t2, a.poly);
+                out[io] = gather_point<K, COMP>(patch, PC, g.Ke, lr, lc, t1, t2, a.poly);
             } else {
                 float w1[W], w2[W], d1[W], d2[W];
                 weights_poly_d<K>(t1, w1, d1, a.poly);
@@ -135,9 +136,9 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                     bx = fmaf(w1[r], qx, bx);
                     by = fmaf(w1[r], qy, by);
                 }
-                const float2 v = __ldg(&vin[raw.w]);
-                g1[raw.w] = a.ds1 * (v.x * ax + v.y * ay);
-                g2[raw.w] = a.ds2 * (v.x * bx + v.y * by);
+                const float2 v = __ldg(&vin[io]);
+                g1[io] = a.ds1 * (v.x * ax + v.y * ay);
+                g2[io] = a.ds2 * (v.x * bx + v.y * by);
             }
         }
         __syncthreads();  // buffer b is free for the prefetch issued next iteration
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
         Cx o;
         o.x = sx;
         o.y = sy;
-        out[r.orig] = o;
+        out[a.binned_io ? i : r.orig] = o;
     } else {
         Real d1[W], d2[W];
         dweights_any<K, Real>(static_cast<Real>(r.t1), w1, d1, a);
@@ -236,13 +237,14 @@ __global__ void __launch_bounds__(kThreads) k_gather_direct(const typename CxOf<
             bx += w1[rr] * qx;
             by += w1[rr] * qy;
         }
-        const Cx v = __ldg(&vin[r.orig]);
+        const int io = a.binned_io ? i : r.orig;
+        const Cx v = __ldg(&vin[io]);
         if constexpr (sizeof(Real) == 4) {
-            g1[r.orig] = a.ds1 * (v.x * ax + v.y * ay);
-            g2[r.orig] = a.ds2 * (v.x * bx + v.y * by);
+            g1[io] = a.ds1 * (v.x * ax + v.y * ay);
+            g2[io] = a.ds2 * (v.x * bx + v.y * by);
         } else {
-            g1[r.orig] = a.ds1_d * (v.x * ax + v.y * ay);
-            g2[r.orig] = a.ds2_d * (v.x * bx + v.y * by);
+            g1[io] = a.ds1_d * (v.x * ax + v.y * ay);
+            g2[io] = a.ds2_d * (v.x * bx + v.y * by);
         }
     }
 }
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, K <= 6 ? 4 : 3)
         latch_error(a.status, kErrBounds);
         return;
     }
-    out[r.orig] = a.compensated ? gather_direct_f32<K, true>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly)
+    out[a.binned_io ? i : r.orig] = a.compensated ? gather_direct_f32<K, true>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly)
                                 : gather_direct_f32<K, false>(grid, g.H, g.C, mu1, mu2, r.t1, r.t2, a.poly);
 }
 
@@ -325,9 +327,10 @@ __global__ void __launch_bounds__(kThreads, K <= 6 ? 3 : 2)
         bx = fmaf(w1[rr], qx, bx);
         by = fmaf(w1[rr], qy, by);
     }
-    const float2 v = __ldg(&vin[r.orig]);
-    g1[r.orig] = a.ds1 * (v.x * ax + v.y * ay);
-    g2[r.orig] = a.ds2 * (v.x * bx + v.y * by);
+    const int io = a.binned_io ? i : r.orig;
+    const float2 v = __ldg(&vin[io]);
+    g1[io] = a.ds1 * (v.x * ax + v.y * ay);
+    g2[io] = a.ds2 * (v.x * bx + v.y * by);
 }
 
 template <typename KernelT>

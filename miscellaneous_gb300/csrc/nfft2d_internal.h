@@ -108,6 +108,7 @@ struct nfft2d_plan_s {
     bool gather_auto = true;     // FP32: pick the gather by bin density at set_points
     int spread_variant = NFFT2D_VARIANT_TILED;
     int compensated = 1;
+    int binned_io = 0;           // per-point arrays (f, v, g) in binned order, see nfft2d_tuning.io_order
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;

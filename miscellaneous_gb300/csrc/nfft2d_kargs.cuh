@@ -16,6 +16,7 @@ struct KArgs {
     int M;                   // points (direct kernels)
     int chunk;               // maximum points per work item of the chunk list
     int compensated;         // FP32 gathers: compensated (TwoSum) sum over the rows
+    int binned_io;           // per-point arrays in the plan's binned order (else the caller's)
     int *status;             // [1]: latched error bits
     WinPoly poly;            // FP32 window polynomials (kernel parameter space)
 };
@@ -35,6 +36,7 @@ inline KArgs make_kargs(const nfft2d_plan_s *p) {
     a.n_chunks = static_cast<int>(p->n_chunks);
     a.M = static_cast<int>(p->M);
     a.compensated = p->compensated;
+    a.binned_io = p->binned_io;
     a.chunk = p->chunk;
     a.status = p->d_status;
     a.poly = p->poly;

@@ -856,6 +856,14 @@ __global__ void k_selftest_wait(uint32_t limit) {
 }  // namespace
 
 namespace nfft2d {
+// perm[i] = the caller's index of the record at binned position i.
+template <typename RecT>
+__global__ void k_record_orig(const RecT *__restrict__ recs, long long M, int *__restrict__ perm) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < M;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        perm[i] = recs[i].orig;
+}
+
 // The same bounded wait latching kErrTimeout into a plan's (or batch's)
 // status word, as the tiled kernels do when their own wait runs out.
 __global__ void k_selftest_latch(uint32_t limit, int *status) {
@@ -1273,6 +1281,10 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     p->gather_auto = gauto;
     p->spread_variant = sv;
     if (t->compensated >= 0) p->compensated = t->compensated ? 1 : 0;
+    if (t->io_order >= 0) {
+        if (t->io_order != NFFT2D_ORDER_CALLER && t->io_order != NFFT2D_ORDER_BINNED) return NFFT2D_ERR_INVALID_ARG;
+        p->binned_io = t->io_order == NFFT2D_ORDER_BINNED;
+    }
     if (t->fft_mode > 2 || t->fft_mode < -1) return NFFT2D_ERR_INVALID_ARG;
     if (t->fft_mode == 2 && !p->fused_ok) return NFFT2D_ERR_UNSUPPORTED;
     if (t->fft_mode >= 0) p->fft_mode = t->fft_mode;
@@ -1599,6 +1611,19 @@ int nfft2d_synchronize(nfft2d_plan p) {
     if (bits) NFFT_TRY_CUDA(cudaMemsetAsync(p->d_status + 1, 0, sizeof(int), p->stream));
     if (bits & kErrTimeout) return NFFT2D_ERR_DEVICE_TIMEOUT;
     if (bits & kErrBounds) return NFFT2D_ERR_DEVICE_BOUNDS;
+    return NFFT2D_OK;
+}
+
+int nfft2d_get_permutation(nfft2d_plan p, int *perm) {
+    if (!p || !perm) return NFFT2D_ERR_INVALID_ARG;
+    if (!p->points_valid) return NFFT2D_ERR_NO_POINTS;
+    if (p->M == 0) return NFFT2D_OK;
+    const int blocks = static_cast<int>(std::min<long long>((p->M + 255) / 256, 65535LL * 16));
+    if (p->precision == NFFT2D_F64)
+        nfft2d::k_record_orig<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->recs), p->M, perm);
+    else
+        nfft2d::k_record_orig<Rec32><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec32 *>(p->recs), p->M, perm);
+    NFFT_TRY_CUDA(cudaGetLastError());
     return NFFT2D_OK;
 }
 

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
         ch.y += first;
         ch.z = min(kSpreadItem, ch.z - first);
         const int tr = ch.x / g.tiles2, tc = ch.x - tr * g.tiles2;
-        spread_item<K>(recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, f, scr, fs, a.poly, a.status);
+        spread_item<K>(recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, f, a.binned_io, scr, fs, a.poly, a.status);
     }
     if (lane == 0) bulk_wait_all();
 }
@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(kThreads) k_spread_direct(Real *__restrict__ g
         latch_error(a.status, kErrBounds);
         return;
     }
-    const Real vx = f[2 * static_cast<size_t>(r.orig)], vy = f[2 * static_cast<size_t>(r.orig) + 1];
+    const size_t io = a.binned_io ? static_cast<size_t>(i) : static_cast<size_t>(r.orig);
+    const Real vx = f[2 * io], vy = f[2 * io + 1];
     Real w1[W], w2[W];
     if constexpr (sizeof(Real) == 4) {
         weights_poly<K>(r.t1, w1, a.poly);

@@ -229,12 +229,13 @@ __device__ __forceinline__ void strip_flush(StripFlush &fs, float2 (&acc)[Spread
 }
 
 // Spread points [first, first + cnt) of one tile (origin r0, c0) into the
-// grid, strip by strip, flushing each strip's register patch.  scr is the
-// warp's scratch of 32 * SpreadGeo<K>::SP floats.  A record outside the tile
-// latches kErrBounds and contributes nothing.
+// grid, strip by strip, flushing each strip's register patch.  f is indexed
+// by the record's caller index, or (binned_io) by the record's position.
+// scr is the warp's scratch of 32 * SpreadGeo<K>::SP floats.  A record
+// outside the tile latches kErrBounds and contributes nothing.
 template <int K>
 __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int first, int cnt, int r0, int c0,
-                                            const float2 *__restrict__ f, float *scr, StripFlush &fs,
+                                            const float2 *__restrict__ f, int binned_io, float *scr, StripFlush &fs,
                                             const WinPoly &wp, int *status) {
     using S = SpreadGeo<K>;
     constexpr int W = S::W, PR = S::PR, SP = S::SP, W1 = S::W1, WV = S::WV;
@@ -256,7 +257,7 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
         if (lane < nb) {
             const int mu1 = static_cast<int>(static_cast<unsigned>(raw.z) >> 16), mu2 = raw.z & 0xFFFF;
             int lr = mu1 - r0, lc = mu2 - c0;
-            float2 v = __ldg(&f[raw.w]);
+            float2 v = __ldg(&f[binned_io ? first + base0 + lane : raw.w]);
             if (static_cast<unsigned>(lr) >= static_cast<unsigned>(kRegTile) ||
                 static_cast<unsigned>(lc) >= static_cast<unsigned>(kRegTile)) {
                 latch_error(status, kErrBounds);

@@ -102,12 +102,22 @@ class Plan:
         check(self._lib.nfft2d_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "nfft2d_set_stream")
 
     def set_tuning(self, tile: int = 0, chunk: int = 0, gather_variant: int = 0, spread_variant: int = 0,
-                   compensated: int = -1, fft_mode: int = -1) -> None:
+                   compensated: int = -1, fft_mode: int = -1, io_order: str | None = None) -> None:
         """fft_mode: -1 keep, 0 cuFFT 2D plan, 1 cuFFT row/band-column passes,
         2 hand-written passes fused with pad/fill/fold/crop (FP32, power-of-two
-        grids; the default below 2048 x 2048 oversampled cells)."""
-        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated, fft_mode)
+        grids; the default below 2048 x 2048 oversampled cells).
+        io_order: None keep, 'caller' or 'binned' (per-point arrays in the
+        plan's binned order, see permutation())."""
+        io = -1 if io_order is None else {"caller": _lib.ORDER_CALLER, "binned": _lib.ORDER_BINNED}[io_order]
+        t = _lib.Tuning(tile, chunk, gather_variant, spread_variant, compensated, fft_mode, io)
         check(self._lib.nfft2d_set_tuning(self._h, ctypes.byref(t)), "nfft2d_set_tuning")
+
+    def permutation(self) -> torch.Tensor:
+        """perm[i] = the caller's index of the point at binned position i (int32,
+        on the device): with io_order 'binned', f_binned = f_caller[perm]."""
+        perm = torch.empty(self.M, dtype=torch.int32, device=torch.device("cuda", torch.cuda.current_device()))
+        check(self._lib.nfft2d_get_permutation(self._h, _ptr(perm)), "nfft2d_get_permutation")
+        return perm
 
     def info(self) -> dict:
         i = _lib.Info()

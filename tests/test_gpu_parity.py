@@ -246,12 +246,16 @@ def test_polar_raster_dense_centre(orc):
     assert orc.rel_l2(adj2, adj) < 1e-6
 
 
-@pytest.mark.parametrize("N1,N2,sigma,prec,tol", [(64, 64, 2.0, "f32", 2e-6), (48, 24, 1.25, "f32", 2e-4),
+@pytest.mark.parametrize("N1,N2,sigma,prec,tol", [(64, 64, 2.0, "f32", 2e-6), (48, 24, 1.25, "f32", 5e-4),
                                                   (16, 64, 2.0, "f64", 1e-13), (512, 256, 2.0, "f32", 2e-6)])
 def test_pruned_fft_matches_full_fft(N1, N2, sigma, prec, tol):
     """The two-pass FFT that skips the zero / cropped columns gives the same
-    transforms as the plain 2D cuFFT plan, within FP32 rounding (amplified up
-    to ~92x by the deapodization at sigma = 1.25, as against the oracle)."""
+    transforms as the plain 2D cuFFT plan, within FP32 rounding.  At
+    sigma = 1.25 the deapodization amplifies the spread's rounding up to ~92x,
+    and the spread's TMA reductions of overlapping strip patches land in a
+    run-dependent order: two runs of the SAME FFT mode differ by up to
+    2.2e-4 there (measured over 8 repetitions on GB300), so the bound sits
+    above that."""
     F, x1, x2, f = _inputs(N1, N2, 3000, seed=21)
     kw = {"sigma": sigma, "K": 6, "precision": prec}
     a = _run(kw, F, x1, x2, f, tuning={"fft_mode": 1})

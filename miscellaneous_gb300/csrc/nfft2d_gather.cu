@@ -54,8 +54,10 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                                                            float *__restrict__ g2,
                                                            const __grid_constant__ KArgs a) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_ok;
+    // full[b]: the TMA of patch buffer b landed (one arrival + its bytes);
+    // empty[b]: every warp is done with buffer b (one arrival per warp)
+    __shared__ __align__(8) uint64_t full[2], empty[2];
+    constexpr int kWarps = kThreads / 32;
     constexpr int W = 2 * K + 1;
     const Geom g = a.g;
     const int PC = CPC > 0 ? CPC : g.PC;
@@ -63,38 +65,47 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
     // TMA shared-memory operands: 128-byte aligned (the launch adds 128 bytes of slack)
     float2 *bufs = reinterpret_cast<float2 *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int n = a.n_chunks >= 0 ? a.n_chunks : a.status[0];  // < 0: counted on the device only
+    const int lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], kWarps);
+        mbar_init(&empty[1], kWarps);
         fence_proxy_async_smem();
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) < n) issue_patch<K>(&tmap, chunks, blockIdx.x, bufs, &bars[0], g);
+    __syncthreads();  // the only CTA-wide barrier: the mbarriers are initialised
+    if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) < n) issue_patch<K>(&tmap, chunks, blockIdx.x, bufs, &full[0], g);
 
-    uint32_t phase = 0;  // bit b: parity to wait for on bars[b]
     int it = 0;
+    int pending = static_cast<int>(blockIdx.x) < n ? 0 : -1;  // thread 0: buffer of the last TMA issued
     for (int c = blockIdx.x; c < n; c += gridDim.x, ++it) {
         const int b = it & 1;
-        const uint32_t par = (phase >> b) & 1u;
         const int cnext = c + gridDim.x;
-        if (threadIdx.x == 0) {
-            if (cnext < n) {
+        bool ok = true;
+        if (threadIdx.x == 0 && cnext < n) {
+            // the next patch goes to buffer b^1 once every warp is done with
+            // its previous use (iteration it - 1)
+            if (it >= 1 && !mbar_wait_bounded(&empty[b ^ 1], ((it - 1) >> 1) & 1u)) {
+                ok = false;
+            } else {
                 fence_proxy_async_smem();
-                issue_patch<K>(&tmap, chunks, cnext, bufs + (b ^ 1) * pstride, &bars[b ^ 1], g);
+                issue_patch<K>(&tmap, chunks, cnext, bufs + (b ^ 1) * pstride, &full[b ^ 1], g);
+                pending = b ^ 1;
             }
-            s_ok = mbar_wait_bounded(&bars[b], par) ? 1 : 0;
         }
-        __syncthreads();
-        if (!s_ok) {
-            if (threadIdx.x == 0) {
-                latch_error(a.status, kErrTimeout);
-                if (cnext < n) (void)mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
-            }
+        // this iteration's patch has landed (each thread acquires it itself)
+        if (ok && !mbar_wait_bounded(&full[b], (it >> 1) & 1u)) ok = false;
+        // a wait that ran out ends the whole warp at once (no lane is left
+        // at a warp barrier); the other warps' own bounded waits then run
+        // out in turn
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) latch_error(a.status, kErrTimeout);
+            // never leave with a copy into this CTA's shared memory in flight
+            if (threadIdx.x == 0 && pending == (b ^ 1) && cnext < n)
+                (void)mbar_wait_bounded(&full[b ^ 1], ((it + 1) >> 1) & 1u);
             return;
         }
-        if (threadIdx.x != 0) (void)mbar_wait_bounded(&bars[b], par);  // completed: acquire only
-        phase ^= (1u << b);
 
         const int4 ch = __ldg(&chunks[c]);
         const int tr = ch.x / g.tiles2, tc = ch.x - tr * g.tiles2;
@@ -141,7 +152,8 @@ __global__ void __launch_bounds__(kThreads, MODE == 0 ? 4 : 2) k_gather_tiled(co
                 g2[io] = a.ds2 * (v.x * bx + v.y * by);
             }
         }
-        __syncthreads();  // buffer b is free for the prefetch issued next iteration
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[b]);  // this warp is done with buffer b
     }
 }
 
@@ -347,7 +359,9 @@ cudaError_t launch_K(const nfft2d_plan_s *p, void *f, const void *v, void *g1, v
         const int smem = 2 * patch_stride_elems(p->g) * static_cast<int>(sizeof(float2)) + 128;
         auto kernel = p->g.PC == 32
                           ? (p->compensated ? k_gather_tiled<K, true, MODE, 32> : k_gather_tiled<K, false, MODE, 32>)
-                          : (p->compensated ? k_gather_tiled<K, true, MODE, 0> : k_gather_tiled<K, false, MODE, 0>);
+                          : p->g.PC == 36
+                                ? (p->compensated ? k_gather_tiled<K, true, MODE, 36> : k_gather_tiled<K, false, MODE, 36>)
+                                : (p->compensated ? k_gather_tiled<K, true, MODE, 0> : k_gather_tiled<K, false, MODE, 0>);
         cudaError_t e = prepare_smem(kernel, smem);
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kThreads, smem);

@@ -928,6 +928,11 @@ int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile,
     // shared-memory banks with fewer conflicts (2.6 instead of 3.1 wavefronts
     // per 64-bit load on the polar and uniform point sets at T = 32, K = 6).
     g->PC = ((T + 2 * g->Ke + 15) / 16) * 16;
+    // Strip-ordered tiles put a warp's consecutive points in SW columns and
+    // many rows; a pitch of SW mod 16 complex shifts each patch row by 2 SW
+    // banks, so the tiled gather's 8-byte tap loads of a half-warp (16
+    // points, 16 / SW rows of SW columns) meet distinct banks.
+    if (g->SW < T) g->PC += g->SW;
     g->R = g->n1 + 2 * kHalo;
     g->Cl = g->n2 + 2 * kHalo;
     // allocation: whole tiles + halo, plus the pitch padding of the last patch

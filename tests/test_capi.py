@@ -70,17 +70,20 @@ def test_layout_query_host_only(lib):
     d = info.as_dict()
     assert (d["n1"], d["n2"]) == (1024, 1024)
     # default 16 x 16 tiles; rows: whole tiles + halo; pitch: + patch pitch pad
-    assert d["halo"] == 8 and (d["rows"], d["cols"]) == (1040, 1044)
     assert d["tile"] == 16 and (d["tiles1"], d["tiles2"]) == (64, 64)
-    # 28 columns needed, pitch rounded up to 16 complex
-    assert (d["patch_rows"], d["patch_cols"]) == (28, 32)
+    # 28 columns needed, pitch rounded up to 16 complex, plus the strip width
+    # (4 at K = 6) so that the rows of a strip-ordered tile meet distinct banks
+    assert (d["patch_rows"], d["patch_cols"]) == (28, 36)
+    assert d["halo"] == 8 and (d["rows"], d["cols"]) == (1040, 1024 + 16 + 36 - 28)
     assert lib.nfft2d_layout_query(512, 512, 2.0, 6, 0, 32, ctypes.byref(info)) == 0
-    assert (info.patch_rows, info.patch_cols, info.cols) == (44, 48, 1044)
+    assert (info.patch_rows, info.patch_cols, info.cols) == (44, 48, 1044)  # 32 x 32 tiles: row-major, no shift
     assert lib.nfft2d_layout_query(22, 22, 2.0, 6, 0, 0, ctypes.byref(info)) == 0
-    assert (info.rows, info.cols, info.tiles1) == (3 * 16 + 16, 3 * 16 + 16 + 4, 3)
+    assert (info.rows, info.cols, info.tiles1) == (3 * 16 + 16, 3 * 16 + 16 + 8, 3)
     # odd K: patch columns are rounded up so every TMA x coordinate is 16-byte aligned
     assert lib.nfft2d_layout_query(64, 64, 2.0, 5, 0, 16, ctypes.byref(info)) == 0
-    assert info.patch_cols == 32 and info.patch_rows == 16 + 10  # 16 + 12 -> 32
+    assert info.patch_cols == 32 + 4 and info.patch_rows == 16 + 10  # 16 + 12 -> 32, + strip width 4
+    assert lib.nfft2d_layout_query(64, 64, 2.0, 8, 0, 16, ctypes.byref(info)) == 0
+    assert info.patch_cols == 32  # K = 8: one strip per tile, plain row-major order
     # the reference test's grid (22 -> 44) gets a partial last tile
     assert lib.nfft2d_layout_query(22, 22, 2.0, 6, 0, 0, ctypes.byref(info)) == 0
     assert info.n1 == 44 and info.tile == 16 and info.tiles1 == 3

@@ -559,39 +559,28 @@ def choose_cpu_sample(wl, max_step_s: float = 1.0):
     return idx, dt
 
 
-def cpu_baseline(wl, target_s: float = 15.0, steps: int | None = None):
-    """Time the CPU restatement on a bounded sample.  When the sample is a
-    subset of the points, a second, 4x smaller sample fixes the model
-    t(m) = a + b m (a: the grid-sized FFT and pad work, b: per point) and the
-    value is the rate that model gives for the full point count."""
-    import oracle
-    oracle.build()
-    cores = oracle.get_threads()
-    M = wl["x1"].size
-    idx, dt = choose_cpu_sample(wl)
-    m = idx.size
-    n = steps if steps is not None else max(1, min(20, int(target_s / max(dt, 1e-3))))
-    t = statistics.median([cpu_reference_step(wl, idx) for _ in range(n)])
-    out = {"unit": UNIT, "cores": cores, "kind": "port", "ms_per_step": t * 1e3, "points": m,
-           "sample_rate": m / t}
-    if m < M:
-        m2 = max(1, m // 4)
-        idx2 = _cpu_sample(wl, np.random.default_rng(321), m2)
-        t2 = statistics.median([cpu_reference_step(wl, idx2) for _ in range(max(3, n // 2))])
-        b = max((t - t2) / (m - m2), 0.0)
-        a = max(t - b * m, 0.0)
-        out["value"] = M / (a + b * M)
-        out["extrapolated"] = True
-        out["model"] = {"grid_s": a, "per_point_s": b, "small_sample_points": m2, "small_sample_ms": t2 * 1e3}
-        how = (f"{m} and {m2} of {M} points (random subsets) with the full {wl['N1']}x{wl['N2']} grid; value is "
-               f"M / (a + b M) from the two medians")
-    else:
-        out["value"] = m / t
-        out["extrapolated"] = False
-        how = f"all {M} points with the full {wl['N1']}x{wl['N2']} grid"
-    out["sample"] = (f"{how}; forward+adjoint per step, median of {n} steps, oracle/nfft2d_oracle.c "
-                     f"(restated NFFT1_2D.m + NFFT2_2D.m, OpenMP)")
-    return out
+def cpu_baseline_isolated(args, steps: int = 10):
+    """The CPU baseline of the library's line, timed by the reference arm's
+    own code (run_reference) in a child process that never creates a CUDA
+    context: the restatement's per-step grids are large fresh allocations,
+    and their page faults cost about twice as much in a process that holds
+    a CUDA context and pinned host buffers, which would make the two arms'
+    CPU figures disagree.  Returns the child's cpu_baseline object."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", args.workload,
+           "--steps", str(steps), "--warmup", "3", "--no-reference-gpu"]
+    if args.K:
+        cmd += ["--K", str(args.K)]
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE")}
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    try:
+        res = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600, check=True)
+        line = json.loads(res.stdout.strip().splitlines()[-1])
+    except (subprocess.SubprocessError, ValueError, IndexError) as e:
+        return {"unavailable": f"CPU baseline child process failed: {type(e).__name__}"}
+    cb = dict(line["cpu_baseline"])
+    cb["ms_per_step"] = line["ms_per_step"]
+    cb["process"] = "child process without a CUDA context (the reference arm's code, --steps %d)" % steps
+    return cb
 
 
 # ---------------------------------------------------------------------------
@@ -899,25 +888,34 @@ def run_ours(args, wl):
         dx1, dx2 = torch.empty_like(x1), torch.empty_like(x2)
         dF, df = torch.empty_like(F), torch.empty_like(f)
         plan.enable_timing(False)
-        # the copies that the compute does not wait for run on a second
-        # stream: F and f go up while set_points bins the points, f_out comes
-        # down while the adjoint runs
+        # The link carries x1, x2, F and f up and f_out, F_out down.  The
+        # binning needs the coordinates first and the forward needs F, so
+        # those go first and alone (concurrent uploads share the link); f
+        # goes up on a second stream while the binning finishes and the
+        # forward runs, and f_out comes down on it while the adjoint runs.
+        # e2e_coords "direct": the binning pass reads the page-locked
+        # coordinates over the link itself (set_points accepts them), so the
+        # upload and the pass overlap; "copy": they are copied first.
         cs = torch.cuda.Stream(device=dev)
-        ev_start, ev_in, ev_fwd, ev_out = (torch.cuda.Event() for _ in range(4))
+        ev_sp, ev_in, ev_fwd, ev_out = (torch.cuda.Event() for _ in range(4))
+        direct = args.e2e_coords == "direct"
 
         def e2e_step():
-            ev_start.record(stream)
-            dx1.copy_(hx1, non_blocking=True)
-            dx2.copy_(hx2, non_blocking=True)
-            cs.wait_event(ev_start)
+            dF.copy_(hF, non_blocking=True)
+            if direct:
+                plan.set_points(hx1, hx2, units="unit", sync=False)
+            else:
+                dx1.copy_(hx1, non_blocking=True)
+                dx2.copy_(hx2, non_blocking=True)
+                plan.set_points(dx1, dx2, units="unit", sync=False)
+            ev_sp.record(stream)
+            cs.wait_event(ev_sp)
             with torch.cuda.stream(cs):
-                dF.copy_(hF, non_blocking=True)
                 df.copy_(hf, non_blocking=True)
                 ev_in.record(cs)
-            plan.set_points(dx1, dx2, units="unit", sync=False)
-            stream.wait_event(ev_in)
             sharded.forward(dF, out=f_out)
             ev_fwd.record(stream)
+            stream.wait_event(ev_in)
             sharded.adjoint(df, out=F_out)
             cs.wait_event(ev_fwd)
             with torch.cuda.stream(cs):
@@ -946,12 +944,27 @@ def run_ours(args, wl):
             te = float(tt.item())
         h2d = (hx1.numel() * 4 + hx2.numel() * 4 + hF.numel() * 8 + hf.numel() * 8)
         d2h = hf_out.numel() * 8 + hF_out.numel() * 8
+        # the coordinates' upload alone (the part of the copies on the
+        # critical path), for the breakdown
+        cu_ms = []
+        for _ in range(3):
+            ev0.record(stream)
+            dx1.copy_(hx1, non_blocking=True)
+            dx2.copy_(hx2, non_blocking=True)
+            ev1.record(stream)
+            ev1.synchronize()
+            cu_ms.append(ev0.elapsed_time(ev1))
+        cu = statistics.median(cu_ms)
         e2e = {"value": world * M / (te * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te,
-               "includes": "H2D copies, set_points (binning sort, enqueued without a host round trip), forward, "
-                           "adjoint, D2H copies; the F/f uploads overlap set_points and the f download overlaps "
-                           "the adjoint (second stream); the plan status is read and L2 is flushed (256 MB "
-                           "written) after each step, outside the events"}
+               "coords_upload_ms": cu, "coords_upload_gbs": (hx1.numel() + hx2.numel()) * 4 / (cu * 1e-3) / 1e9,
+               "coords": args.e2e_coords,
+               "includes": "H2D of F, the coordinates (read by the binning pass over the link with coords "
+                           "'direct', copied first with 'copy') and f, set_points (binning sort, enqueued "
+                           "without a host round trip), forward, adjoint, D2H of f_out and F_out; f goes up "
+                           "during the binning's tail and the forward, f_out comes down during the adjoint "
+                           "(second stream); the plan status is read and L2 is flushed (256 MB written) after "
+                           "each step, outside the events"}
         # restore the resident plan state for the accuracy check
         plan.set_points(x1, x2, units="unit")
 
@@ -1044,7 +1057,7 @@ def run_ours(args, wl):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(wl)
+        cpu = cpu_baseline_isolated(args)
 
     fused = plan.info()["fft_mode"] == 2
     if rank == 0:
@@ -1598,6 +1611,9 @@ def main():
                          "cuFFT passes, fused")
     ap.add_argument("--io-order", choices=["caller", "binned"], default="caller",
                     help="per-point arrays of the timed steps in the caller's or the plan's binned order")
+    ap.add_argument("--e2e-coords", choices=["direct", "copy"], default="direct",
+                    help="e2e: the binning reads the page-locked coordinates over the link (direct) or after "
+                         "a copy (copy)")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
     ap.add_argument("--K", type=int, default=None,

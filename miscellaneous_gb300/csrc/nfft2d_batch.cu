@@ -231,10 +231,10 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float2 *bufs = reinterpret_cast<float2 *>(base) + warp * S::NBUF * S::PATCH;
     float *scr = reinterpret_cast<float *>(reinterpret_cast<float2 *>(base) + kSpreadWarps * S::NBUF * S::PATCH) +
-                 warp * 32 * S::SP;
+                 warp * S::ROWS * S::SP;
     const int parts = (chunk + kSpreadItem - 1) / kSpreadItem;
     StripFlush fs{nullptr, bufs, g0.H, 0};
-    strip_flush_init<K>(fs);
+    strip_flush_init<K>(fs, scr);
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(work, 1);
@@ -632,14 +632,27 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
     b->points_valid = false;
     drop_graphs(b);
     B_TRY(cudaStreamSynchronize(b->stream));
+    // every transform's binning is enqueued on the batch stream without a
+    // host round trip, then the status words (work-item counts, errors) of
+    // all of them come back with one synchronisation
+    for (int i = 0; i < b->count; ++i) {  // internal order; the arguments are in the caller's
+        const int t = b->order[i];
+        const int st = nfft2d_set_points_async(b->plans[i], M[t], x1[t], x2[t], coord_dtype, units);
+        if (st != NFFT2D_OK) return st;
+    }
+    for (int i = 0; i < b->count; ++i)
+        B_TRY(cudaMemcpyAsync(b->plans[i]->h_status, b->plans[i]->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost,
+                              b->stream));
+    B_TRY(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < b->count; ++i) {
+        const int st = apply_status(b->plans[i]);
+        if (st != NFFT2D_OK) return st;
+    }
     std::vector<BatchDesc> h(b->count);
     int chunks = 0, rows = 0, crop = 0;
     long long points = 0;
-    for (int i = 0; i < b->count; ++i) {  // internal order; the arguments are in the caller's
-        const int t = b->order[i];
+    for (int i = 0; i < b->count; ++i) {
         nfft2d_plan_s *p = b->plans[i];
-        const int st = nfft2d_set_points(p, M[t], x1[t], x2[t], coord_dtype, units);
-        if (st != NFFT2D_OK) return st;
         BatchDesc &D = h[i];
         std::memset(&D, 0, sizeof(D));
         std::memcpy(&D.tmap, &p->tmap_spread, sizeof(CUtensorMap));

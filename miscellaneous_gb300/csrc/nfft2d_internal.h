@@ -14,7 +14,6 @@ namespace nfft2d {
 constexpr int kHalo = 8;          // periodic halo around the oversampled grid (>= K rounded up to even)
 constexpr int kMinK = 2;
 constexpr int kMaxK = 8;
-constexpr unsigned kInvalidKey = 0xFFFFFFFFu;
 
 // Device-side error bits latched in Plan::d_status[1].
 constexpr int kErrTimeout = 1;
@@ -130,8 +129,9 @@ struct nfft2d_plan_s {
     bool points_valid = false;
     long long capM = 0;
     void *recs = nullptr;        // sorted Rec32/Rec64
-    void *tmp_recs = nullptr;    // unsorted records, key in .orig
-    unsigned *ranks = nullptr;
+    void *tmp_recs = nullptr;    // unsorted records (caller order)
+    uint2 *keyrank = nullptr;    // per point: cell key, rank within the cell
+    int *src = nullptr;          // per sorted position: the caller index
     int4 *chunks = nullptr;
     long long chunks_cap = 0;
     long long n_chunks = 0;
@@ -190,6 +190,13 @@ int tensor_map_for(nfft2d_plan_s *p);
 // until nfft2d_synchronize reads it back with the error bits.
 int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype, double u1,
                       double u2, double o1, double o2, bool async = false);
+
+// After the plan's status words were copied to p->h_status and its stream
+// went idle: completes a set_points enqueued by nfft2d_set_points_async
+// (the work-item count) and reports, then clears, the latched device-side
+// error bits -- the tail of nfft2d_synchronize, for callers that fetch
+// many plans' status words with one synchronisation.
+int apply_status(nfft2d_plan_s *p);
 
 // A type-2 transform whose deapodized, zero-padded coefficients are written
 // into the grid interior by `pad` (launched on the plan's stream, timed as

@@ -488,7 +488,7 @@ __device__ __forceinline__ bool reduce_coord(CT x, double o, double s, float sf,
 template <typename CT, typename RecT>
 __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double o1, double o2,
                             double s1, double s2, float s1f, float s2f, int exact_f32, Geom g, RecT *__restrict__ tmp,
-                            unsigned *__restrict__ ranks, unsigned *__restrict__ cell_count,
+                            uint2 *__restrict__ keyrank, unsigned *__restrict__ cell_count,
                             int *__restrict__ status, unsigned long long *__restrict__ scan_state,
                             int scan_words) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -515,21 +515,31 @@ __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2
                          static_cast<unsigned>((st * g.T + lr) * g.SW + sc);
     const unsigned rank = atomicAdd(cell_count + key, 1u);
     r.mu = (mu1 << 16) | mu2;
-    r.orig = static_cast<int>(key);
+    r.orig = i;
     tmp[i] = r;
-    ranks[i] = rank;
+    keyrank[i] = make_uint2(key, rank);
 }
 
-template <typename RecT>
-__global__ void k_bin_scatter(const RecT *__restrict__ tmp, const unsigned *__restrict__ ranks,
-                              const unsigned *__restrict__ cell_start, int M, RecT *__restrict__ recs) {
+// The sorted position of every point, inverted: src[cell_start[key] + rank]
+// = i.  The 4-byte writes land in an array a quarter of the records' size,
+// which stays in L2 where the writes merge into whole lines.
+__global__ void k_bin_invert(const uint2 *__restrict__ keyrank, const unsigned *__restrict__ cell_start, int M,
+                             int *__restrict__ src) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
-    RecT r = tmp[i];
-    const unsigned key = static_cast<unsigned>(r.orig);
-    if (key == kInvalidKey) return;
-    r.orig = i;
-    recs[cell_start[key] + ranks[i]] = r;
+    const uint2 kr = __ldg(keyrank + i);
+    src[cell_start[kr.x] + kr.y] = i;
+}
+
+// recs[p] = tmp[src[p]]: the records move to their sorted positions as
+// random reads and coalesced writes (a scatter of the 16-byte records would
+// write half sectors at random addresses of an array larger than L2).
+template <typename RecT>
+__global__ void k_bin_gather(const RecT *__restrict__ tmp, const int *__restrict__ src, int M,
+                             RecT *__restrict__ recs) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= M) return;
+    recs[q] = tmp[__ldg(src + q)];
 }
 
 // ---------------------------------------------------------------------------
@@ -706,10 +716,12 @@ __global__ void __launch_bounds__(kItemScanThreads, 1) k_scan_emit_chunks(const 
 void free_points(nfft2d_plan_s *p) {
     cudaFree(p->recs);
     cudaFree(p->tmp_recs);
-    cudaFree(p->ranks);
+    cudaFree(p->keyrank);
+    cudaFree(p->src);
     cudaFree(p->chunks);
     p->recs = p->tmp_recs = nullptr;
-    p->ranks = nullptr;
+    p->keyrank = nullptr;
+    p->src = nullptr;
     p->chunks = nullptr;
     p->capM = 0;
     p->chunks_cap = 0;
@@ -749,7 +761,8 @@ int ensure_points_capacity(nfft2d_plan_s *p, long long M) {
     const size_t rs = rec_size(p->precision);
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->recs), rs * cap));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->tmp_recs), rs * cap));
-    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->ranks), sizeof(unsigned) * cap));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->keyrank), sizeof(uint2) * cap));
+    NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->src), sizeof(int) * cap));
     const long long cc = chunks_capacity(p, cap);
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->chunks), sizeof(int4) * cc));
     p->capM = cap;
@@ -759,7 +772,7 @@ int ensure_points_capacity(nfft2d_plan_s *p, long long M) {
 
 size_t plan_workspace_bytes(const nfft2d_plan_s *p) {
     const size_t grid = cplx_size(p->precision) * static_cast<size_t>(p->g.Ra) * p->g.C;
-    const size_t pts = static_cast<size_t>(p->capM) * (2 * rec_size(p->precision) + sizeof(unsigned)) +
+    const size_t pts = static_cast<size_t>(p->capM) * (2 * rec_size(p->precision) + sizeof(uint2) + sizeof(int)) +
                        static_cast<size_t>(p->chunks_cap) * sizeof(int4);
     const size_t bins = sizeof(unsigned) * (p->ncells + 1 + p->scan_tmp_elems);
     return grid + pts + bins + real_size(p->precision) * (p->N1 + p->N2);
@@ -856,14 +869,6 @@ __global__ void k_selftest_wait(uint32_t limit) {
 }  // namespace
 
 namespace nfft2d {
-// perm[i] = the caller's index of the record at binned position i.
-template <typename RecT>
-__global__ void k_record_orig(const RecT *__restrict__ recs, long long M, int *__restrict__ perm) {
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < M;
-         i += static_cast<long long>(gridDim.x) * blockDim.x)
-        perm[i] = recs[i].orig;
-}
-
 // The same bounded wait latching kErrTimeout into a plan's (or batch's)
 // status word, as the tiled kernels do when their own wait runs out.
 __global__ void k_selftest_latch(uint32_t limit, int *status) {
@@ -1419,32 +1424,34 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec64><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
+                static_cast<Rec64 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
         else
             k_bin_pass1<float, Rec64><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec64 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
+                static_cast<Rec64 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
     } else {
         if (coord_dtype == NFFT2D_COORD_F64)
             k_bin_pass1<double, Rec32><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
+                static_cast<Rec32 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
         else
             k_bin_pass1<float, Rec32><<<blocks, 256, 0, p->stream>>>(
                 static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec32 *>(p->tmp_recs), p->ranks, p->cell_count, p->d_status, scan_state, scan_words);
+                static_cast<Rec32 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
     }
     NFFT_TRY_CUDA(cudaGetLastError());
     const size_t cells_n = p->ncells + 1;
     k_scan_counts<<<static_cast<unsigned>((cells_n + kCellTile - 1) / kCellTile), kCellScanThreads, 0, p->stream>>>(
         p->cell_count, cells_n, scan_state, p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
+    k_bin_invert<<<blocks, 256, 0, p->stream>>>(p->keyrank, p->cell_count, Mi, p->src);
+    NFFT_TRY_CUDA(cudaGetLastError());
     if (p->precision == NFFT2D_F64)
-        k_bin_scatter<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->tmp_recs), p->ranks,
-                                                            p->cell_count, Mi, static_cast<Rec64 *>(p->recs));
+        k_bin_gather<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->tmp_recs), p->src, Mi,
+                                                           static_cast<Rec64 *>(p->recs));
     else
-        k_bin_scatter<Rec32><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec32 *>(p->tmp_recs), p->ranks,
-                                                            p->cell_count, Mi, static_cast<Rec32 *>(p->recs));
+        k_bin_gather<Rec32><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec32 *>(p->tmp_recs), p->src, Mi,
+                                                           static_cast<Rec32 *>(p->recs));
     NFFT_TRY_CUDA(cudaGetLastError());
     const int ntiles = g.tiles1 * g.tiles2;
     k_scan_emit_chunks<<<static_cast<unsigned>((ntiles + 1 + kItemTile - 1) / kItemTile), kItemScanThreads, 0,
@@ -1596,10 +1603,18 @@ static int nfft2d_grad_x_impl(nfft2d_plan p, int sign, const void *F, const void
 
 int nfft2d_synchronize(nfft2d_plan p) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
-    const int *hs = p->h_status;
     NFFT_TRY_CUDA(cudaMemcpyAsync(p->h_status, p->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
     NFFT_TRY_CUDA(cudaStreamSynchronize(p->stream));
     NFFT_TRY_CUDA(cudaGetLastError());
+    return nfft2d::apply_status(p);
+}
+}  // extern "C"
+
+// The status words already copied to p->h_status (the stream idle since):
+// completes an asynchronous set_points and reports (then clears) the
+// device-side error bits.
+int nfft2d::apply_status(nfft2d_plan_s *p) {
+    const int *hs = p->h_status;
     if (p->points_valid && p->n_chunks < 0) {  // points set by nfft2d_set_points_async
         if (hs[1] & kErrNonfinite) {
             p->points_valid = false;
@@ -1619,16 +1634,14 @@ int nfft2d_synchronize(nfft2d_plan p) {
     return NFFT2D_OK;
 }
 
+extern "C" {
 int nfft2d_get_permutation(nfft2d_plan p, int *perm) {
     if (!p || !perm) return NFFT2D_ERR_INVALID_ARG;
     if (!p->points_valid) return NFFT2D_ERR_NO_POINTS;
     if (p->M == 0) return NFFT2D_OK;
-    const int blocks = static_cast<int>(std::min<long long>((p->M + 255) / 256, 65535LL * 16));
-    if (p->precision == NFFT2D_F64)
-        nfft2d::k_record_orig<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->recs), p->M, perm);
-    else
-        nfft2d::k_record_orig<Rec32><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec32 *>(p->recs), p->M, perm);
-    NFFT_TRY_CUDA(cudaGetLastError());
+    // the binning's inverse permutation is exactly this array
+    NFFT_TRY_CUDA(cudaMemcpyAsync(perm, p->src, sizeof(int) * static_cast<size_t>(p->M), cudaMemcpyDeviceToDevice,
+                                  p->stream));
     return NFFT2D_OK;
 }
 

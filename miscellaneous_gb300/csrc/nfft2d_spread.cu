@@ -58,11 +58,11 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float2 *bufs = reinterpret_cast<float2 *>(base) + warp * S::NBUF * S::PATCH;
     float *scr = reinterpret_cast<float *>(reinterpret_cast<float2 *>(base) + kSpreadWarps * S::NBUF * S::PATCH) +
-                 warp * 32 * S::SP;
+                 warp * S::ROWS * S::SP;
     const int n = a.n_chunks >= 0 ? a.n_chunks : a.status[0];  // < 0: counted on the device only
     int *work = a.status + 2;  // work-item counter, zeroed before the launch
     StripFlush fs{&tmap, bufs, g.H, 0};
-    strip_flush_init<K>(fs);
+    strip_flush_init<K>(fs, scr);
 
     const int parts = (a.chunk + kSpreadItem - 1) / kSpreadItem;  // items per chunk
     for (;;) {

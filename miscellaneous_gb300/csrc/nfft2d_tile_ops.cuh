@@ -143,15 +143,20 @@ struct SpreadGeo {
     static constexpr int BOXC = G + 2 * ODD;            // shared patch / TMA box columns (complex)
     static constexpr int NBUF = NG;                     // flush buffers per warp: one per group
     static constexpr int W1 = ((W + 3) / 4) * 4;        // floats of the row weights (padded)
-    static constexpr int WV = ((2 * W + 3) / 4) * 4;    // floats of the column products v * w2
+    static constexpr int WV = 2 * G;                    // floats of the lane-aligned column products
     // per-point scratch (floats): {lr, strip column, strip, -}, the row
-    // weights, the column products as float2.  The stride is 4 mod 8: the
+    // weights, then one float2 per group lane: the lane's column product
+    // v * w2 (zero outside the point's 2K+1 columns), so a lane loads its
+    // operand at a fixed offset with no test.  The stride is 4 mod 8: the
     // prepass's 16-byte stores of 8 consecutive lanes hit 8 distinct bank
     // quads, and the groups' loads of consecutive points hit distinct banks.
     // (A shared-memory load costs about one wavefront per float it delivers
     // whatever its width, so the row weights are stored once and broadcast.)
+    // Row 32, after the batch's 32 points, stays zero: a group without a
+    // point in a step reads it and adds zeros.
     static constexpr int SP0 = 4 + W1 + WV;
     static constexpr int SP = SP0 % 8 == 0 ? SP0 + 4 : SP0;
+    static constexpr int ROWS = 33;                     // scratch rows per warp (32 points + the zero row)
     static constexpr int PATCH = ((PR * BOXC + 15) / 16) * 16;  // float2 per buffer, 128-byte multiple
     static_assert(SW + 2 * K <= G, "strip windows must fit the group");
     static_assert(kRegTile % SW == 0, "strips tile the tile");
@@ -161,7 +166,7 @@ struct SpreadGeo {
 template <int K>
 __host__ __device__ constexpr int spread_warp_smem_bytes() {
     using S = SpreadGeo<K>;
-    return S::NBUF * S::PATCH * 8 + 32 * S::SP * 4;
+    return S::NBUF * S::PATCH * 8 + S::ROWS * S::SP * 4;
 }
 
 // acc[L + a] += (ax, ay) * w1[a] for the 2K+1 rows of a point whose first
@@ -194,12 +199,13 @@ struct StripFlush {
 };
 
 // Zero the warp's patch buffers once (odd K: the columns outside the lanes
-// stay zero for the life of the kernel).
+// stay zero for the life of the kernel) and the zero row of its scratch scr.
 template <int K>
-__device__ __forceinline__ void strip_flush_init(StripFlush &fs) {
+__device__ __forceinline__ void strip_flush_init(StripFlush &fs, float *scr) {
     using S = SpreadGeo<K>;
     const int lane = threadIdx.x & 31;
     for (int i = lane; i < S::NBUF * S::PATCH; i += 32) fs.bufs[i] = make_float2(0.f, 0.f);
+    for (int i = lane; i < S::SP; i += 32) scr[32 * S::SP + i] = 0.f;
     __syncwarp();
 }
 
@@ -231,14 +237,14 @@ __device__ __forceinline__ void strip_flush(StripFlush &fs, float2 (&acc)[Spread
 // Spread points [first, first + cnt) of one tile (origin r0, c0) into the
 // grid, strip by strip, flushing each strip's register patch.  f is indexed
 // by the record's caller index, or (binned_io) by the record's position.
-// scr is the warp's scratch of 32 * SpreadGeo<K>::SP floats.  A record
+// scr is the warp's scratch of SpreadGeo<K>::ROWS * SP floats.  A record
 // outside the tile latches kErrBounds and contributes nothing.
 template <int K>
 __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int first, int cnt, int r0, int c0,
                                             const float2 *__restrict__ f, int binned_io, float *scr, StripFlush &fs,
                                             const WinPoly &wp, int *status) {
     using S = SpreadGeo<K>;
-    constexpr int W = S::W, PR = S::PR, SP = S::SP, W1 = S::W1, WV = S::WV;
+    constexpr int W = S::W, PR = S::PR, SP = S::SP, W1 = S::W1;
     const int lane = threadIdx.x & 31;
     const int grp = lane / S::G, gl = lane % S::G;
     float2 acc[PR];
@@ -270,26 +276,28 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
             weights_poly<K>(__int_as_float(raw.x), w1, wp);
             weights_poly<K>(__int_as_float(raw.y), w2, wp);
             float *sp = scr + lane * SP;
-            reinterpret_cast<int4 *>(sp)[0] = make_int4(lr, lc - st * S::SW, st, 0);
+            const int q = lc - st * S::SW;  // first patch column of the point within the strip
+            reinterpret_cast<int4 *>(sp)[0] = make_int4(lr, q, st, 0);
             float4 *wq = reinterpret_cast<float4 *>(sp + 4);
 #pragma unroll
             for (int k = 0; k < W1 / 4; ++k)
                 wq[k] = make_float4(w1[4 * k], 4 * k + 1 < W ? w1[4 * k + 1] : 0.f,
                                     4 * k + 2 < W ? w1[4 * k + 2] : 0.f, 4 * k + 3 < W ? w1[4 * k + 3] : 0.f);
+            // the group lanes' column products: zeros, then the 2K+1
+            // products at lanes q .. q+2K (q + 2K < G)
             float4 *vq = reinterpret_cast<float4 *>(sp + 4 + W1);
 #pragma unroll
-            for (int k = 0; k < WV / 4; ++k) {
-                const float a = 2 * k < W ? w2[2 * k] : 0.f;
-                const float b = 2 * k + 1 < W ? w2[2 * k + 1] : 0.f;
-                vq[k] = make_float4(v.x * a, v.y * a, v.x * b, v.y * b);
-            }
+            for (int k = 0; k < S::WV / 4; ++k) vq[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 *vl = reinterpret_cast<float2 *>(sp + 4 + W1) + q;
+#pragma unroll
+            for (int b = 0; b < W; ++b) vl[b] = make_float2(v.x * w2[b], v.y * w2[b]);
         }
         if (base0 + 32 + lane < cnt) raw_next = __ldg(reinterpret_cast<const int4 *>(recs) + first + base0 + 32 + lane);
         __syncwarp();
-        // 2) operands of point p for this lane: the row weights (broadcast
-        //    within the group) and this lane's column product (zero outside
-        //    the point's columns, or when the group has no point this step)
-        auto load = [&](int p, bool ok, float (&w1)[W], float2 &vw) {
+        // 2) operands of scratch row p for this lane: the row weights
+        //    (broadcast within the group) and this lane's column product
+        //    (row 32 is all zeros: the group has no point this step)
+        auto load = [&](int p, float (&w1)[W], float2 &vw) {
             const float *sp = scr + p * SP;
             const float4 *wq = reinterpret_cast<const float4 *>(sp + 4);
 #pragma unroll
@@ -302,9 +310,7 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
             }
 #pragma unroll
             for (int a = (W / 4) * 4; a < W; ++a) w1[a] = sp[4 + a];
-            const int b = gl - reinterpret_cast<const int *>(sp)[1];
-            vw = (ok && static_cast<unsigned>(b) < static_cast<unsigned>(W))
-                     ? reinterpret_cast<const float2 *>(sp + 4 + W1)[b] : make_float2(0.f, 0.f);
+            vw = reinterpret_cast<const float2 *>(sp + 4 + W1)[gl];
         };
         // The binning keeps a work item's keys ascending; a batch out of
         // order can only follow a record that failed the bounds check above
@@ -338,10 +344,9 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
                     const int n = __popc(__ballot_sync(0xffffffffu, my_key == ((st << 4) | L)));
 #pragma unroll 1
                     for (int k = 0; k < n; k += S::NG) {
-                        const bool ok = k + grp < n;
                         float w1[W];
                         float2 vw;
-                        load(ok ? j + k + grp : j, ok, w1, vw);
+                        load(k + grp < n ? j + k + grp : 32, w1, vw);
                         add_rows2<K, PR, L>(acc, w1, vw);
                     }
                     j += n;

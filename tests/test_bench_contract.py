@@ -37,3 +37,16 @@ def test_reference_arm_line():
 def test_reference_arm_unavailable_workload():
     d = _run("--impl", "reference", "--workload", "batch", "--steps", "1")
     assert d["impl"] == "reference" and d["unavailable"]
+
+
+def test_library_line_cpu_baseline_is_the_reference_arm_in_a_child():
+    """The library line's cpu_baseline comes from the reference arm's code run
+    in a child process without a CUDA context (both arms' CPU figures are
+    then one measurement method)."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    cb = bench.cpu_baseline_isolated(argparse.Namespace(workload="config1", K=None), steps=1)
+    assert "unavailable" not in cb, cb
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1 and cb["sample"]
+    assert cb["extrapolated"] is False and "child process" in cb["process"]

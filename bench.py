@@ -356,8 +356,23 @@ def ffbp_scene(seed: int = 7, Np: int = 64, nf: int = 216, Nx: int = 128, step: 
                         "targets": len(targets), "seed": seed})
 
 
+def type3_scene(seed: int = 8, M: int = 1 << 20, N: int = 1 << 20, eps: float = 1e-6):
+    """Type-3 2D NUFFT (NUFFT_2D_CPU's problem): M nonuniform points with
+    x ~ U(-40, 25), y ~ N(0, 6^2) and complex N(0, 1) values, N nonuniform
+    frequencies s ~ U(-3, 4), t ~ U(-2.5, 2.5) (seeded PCG64), accuracy eps."""
+    rng = np.random.default_rng(seed)
+    x, y = rng.uniform(-40.0, 25.0, M), rng.normal(0.0, 6.0, M)
+    f = (rng.standard_normal(M) + 1j * rng.standard_normal(M)).astype(np.complex64)
+    s, t = rng.uniform(-3.0, 4.0, N), rng.uniform(-2.5, 2.5, N)
+    return dict(name=f"type3_{M}_{N}", x=x, y=y, f=f, s=s, t=t, eps=eps,
+                config={"workload": "type-3 2D NUFFT (Gaussian gridding)", "points": M, "frequencies": N,
+                        "eps": eps, "x": "U(-40, 25)", "y": "N(0, 6^2)", "s": "U(-3, 4)", "t": "U(-2.5, 2.5)",
+                        "seed": seed})
+
+
 WORKLOADS = {"polar": polar_raster, "config1": uniform_config1, "clustered": clustered_config3, "batch": uneven_batch,
-             "lsq": least_squares_config5, "knab": knab_regrid, "pso": pso_batch, "ffbp": ffbp_scene}
+             "lsq": least_squares_config5, "knab": knab_regrid, "pso": pso_batch, "ffbp": ffbp_scene,
+             "type3": type3_scene}
 
 
 # ---------------------------------------------------------------------------
@@ -1591,6 +1606,128 @@ def run_ffbp_reference(args, wl):
     print(json.dumps(line))
 
 
+TYPE3_METRIC = "type-3 2D NUFFT: NU points/s (input points + output frequencies) per transform"
+
+
+def type3_cpu_rate(wl, m: int = 1 << 16, reps: int = 3):
+    """The oracle's restatement of NUFFT_2D_CPU (OpenMP on all host cores) on
+    m points and m frequencies drawn from the workload and on m/4 of each,
+    t(m) = a + b m; value = the model's rate for the full sizes.  The
+    reference's own NFFT3_2D_C.cpp needs Intel MKL and FFTW (absent)."""
+    import oracle
+    oracle.build()
+    M, N = wl["x"].size, wl["s"].size
+    rng = np.random.default_rng(1234)
+
+    def step(k):
+        i = np.sort(rng.choice(M, k, replace=False))
+        j = np.sort(rng.choice(N, k, replace=False))
+        args = (wl["x"][i], wl["y"][i], wl["f"][i].astype(np.complex128), wl["s"][j], wl["t"][j])
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            _, info = oracle.nufft3_2d(*args, eps=wl["eps"])
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts), info
+
+    t1, info = step(m)
+    t2, _ = step(m // 4)
+    b = max((t1 - t2) / (2 * (m - m // 4)), 0.0)
+    a = max(t1 - b * 2 * m, 0.0)
+    value = (M + N) / (a + b * (M + N))
+    return {"value": value, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port", "extrapolated": True,
+            "model": {"fixed_s": a, "per_point_s": b, "sample": m, "small_sample": m // 4,
+                      "sample_ms": t1 * 1e3, "grid": [info["Mry"], info["Mrx"]], "msp": info["msp"]},
+            "sample": (f"{m} points + {m} frequencies drawn from the workload (and {m // 4} + {m // 4}), median of "
+                       f"{reps}; oracle/nfft2d_oracle.c restates NUFFT_2D_CPU (NFFT3_2D_C.cpp:199-312), FP64, "
+                       "OpenMP; the reference's own code needs Intel MKL and FFTW, absent here")}
+
+
+def run_type3(args, wl):
+    import torch
+
+    from miscellaneous_gb300.nufft3 import NUFFT_2D
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    M, N = wl["x"].size, wl["s"].size
+    x, y, s, t = (torch.from_numpy(wl[k]).to(dev) for k in ("x", "y", "s", "t"))
+    f = torch.from_numpy(wl["f"]).to(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        NUFFT_2D(x, y, s, t, f, wl["eps"], stream=stream)
+    torch.cuda.synchronize()
+    ms = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            ev0.record(stream)
+            F = NUFFT_2D(x, y, s, t, f, wl["eps"], stream=stream)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+    tm = statistics.median(ms)
+    # e2e: host arrays in, F out
+    e2e = None
+    if not args.no_e2e:
+        hx, hy, hs, ht = (torch.from_numpy(wl[k]).pin_memory() for k in ("x", "y", "s", "t"))
+        hf = torch.from_numpy(wl["f"]).pin_memory()
+        hF = torch.empty(N, dtype=torch.complex64).pin_memory()
+        dx, dy, ds, dt_ = (torch.empty_like(v) for v in (x, y, s, t))
+        df = torch.empty_like(f)
+        em = []
+        for r in range(args.warmup + args.steps):
+            flush.zero_()
+            ev0.record(stream)
+            for d, h in ((dx, hx), (dy, hy), (df, hf), (ds, hs), (dt_, ht)):
+                d.copy_(h, non_blocking=True)
+            Fd = NUFFT_2D(dx, dy, ds, dt_, df, wl["eps"], stream=stream)
+            hF.copy_(Fd, non_blocking=True)
+            ev1.record(stream)
+            ev1.synchronize()
+            if r >= args.warmup:
+                em.append(ev0.elapsed_time(ev1))
+        te = statistics.median(em)
+        e2e = {"value": (M + N) / (te * 1e-3), "unit": UNIT, "ms_per_step": te,
+               "h2d_bytes_per_step": 16 * M + 8 * M + 16 * N, "d2h_bytes_per_step": 8 * N}
+    accuracy = None
+    if not args.no_accuracy:
+        # exact FP64 sums for 512 of the frequencies (torch complex128 on the GPU)
+        sel = torch.from_numpy(np.random.default_rng(99).choice(N, 512, replace=False)).to(dev)
+        fe = f.to(torch.complex128)
+        ref = torch.empty(512, dtype=torch.complex128, device=dev)
+        for c0 in range(0, 512, 32):
+            k = sel[c0:c0 + 32]
+            ph = torch.outer(s[k], x) + torch.outer(t[k], y)
+            ref[c0:c0 + 32] = torch.polar(torch.ones_like(ph), -ph) @ fe
+        got = F[sel].to(torch.complex128)
+        accuracy = {"rel_l2": float(torch.linalg.vector_norm(got - ref) / torch.linalg.vector_norm(ref)),
+                    "frequencies_checked": 512, "oracle": "exact FP64 sum over all points (torch complex128)"}
+    cpu = None if args.no_cpu_baseline else type3_cpu_rate(wl)
+    line = {"metric": TYPE3_METRIC, "value": (M + N) / (tm * 1e-3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tm, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(wl["config"], l2="256 MB buffer written before each timed call"),
+            "step": "one nfft2d_nufft3_2d call (extents, grid allocation, spread, cuFFT, gather; synchronous), "
+                    "CUDA events around it",
+            "accuracy": accuracy, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks.summary()}
+    print(json.dumps(line))
+
+
+def run_type3_reference(args, wl):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cb = type3_cpu_rate(wl)
+    line = {"impl": "reference", "metric": TYPE3_METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
+            "steps": 3, "warmup": 0, "ms_per_step": (wl["x"].size + wl["s"].size) / cb["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": wl["config"], "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1628,6 +1765,12 @@ def main():
             run_ffbp_reference(args, wl)
         else:
             run_ffbp(args, wl)
+        return
+    if args.workload == "type3":
+        if args.impl == "reference":
+            run_type3_reference(args, wl)
+        else:
+            run_type3(args, wl)
         return
     if args.workload == "knab":
         if args.impl == "reference":

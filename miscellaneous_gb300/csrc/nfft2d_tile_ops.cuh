@@ -143,20 +143,27 @@ struct SpreadGeo {
     static constexpr int BOXC = G + 2 * ODD;            // shared patch / TMA box columns (complex)
     static constexpr int NBUF = NG;                     // flush buffers per warp: one per group
     static constexpr int W1 = ((W + 3) / 4) * 4;        // floats of the row weights (padded)
-    static constexpr int WV = 2 * G;                    // floats of the lane-aligned column products
+    // Column products v * w2 in the per-point scratch, either
+    //  - lane-aligned (ALIGNED): one float2 per group lane, zero outside the
+    //    point's 2K+1 columns, so a lane loads its operand at a fixed offset
+    //    with no test; a zero row after the batch's 32 points serves a group
+    //    without a point in a step.  Costs a zero fill and scattered stores
+    //    in the prepass: it pays at K = 5..7 (13 x 13 taps: 72.9 -> 68.2 us
+    //    per 2^20 polar points) but not at K = 4 or 8 (config-3 steps 3 %
+    //    and 7 % slower: fewer taps per store, or 32-lane rows);
+    //  - or packed (the 2K+1 products), each lane indexing them by its
+    //    offset from the point's first column and testing the range.
+    static constexpr bool ALIGNED = G == 16 && W >= 11;
+    static constexpr int WV = ALIGNED ? 2 * G : ((2 * W + 3) / 4) * 4;
     // per-point scratch (floats): {lr, strip column, strip, -}, the row
-    // weights, then one float2 per group lane: the lane's column product
-    // v * w2 (zero outside the point's 2K+1 columns), so a lane loads its
-    // operand at a fixed offset with no test.  The stride is 4 mod 8: the
-    // prepass's 16-byte stores of 8 consecutive lanes hit 8 distinct bank
-    // quads, and the groups' loads of consecutive points hit distinct banks.
-    // (A shared-memory load costs about one wavefront per float it delivers
+    // weights, the column products.  The stride is 4 mod 8: the prepass's
+    // 16-byte stores of 8 consecutive lanes hit 8 distinct bank quads, and
+    // the groups' loads of consecutive points hit distinct banks.  (A
+    // shared-memory load costs about one wavefront per float it delivers
     // whatever its width, so the row weights are stored once and broadcast.)
-    // Row 32, after the batch's 32 points, stays zero: a group without a
-    // point in a step reads it and adds zeros.
     static constexpr int SP0 = 4 + W1 + WV;
     static constexpr int SP = SP0 % 8 == 0 ? SP0 + 4 : SP0;
-    static constexpr int ROWS = 33;                     // scratch rows per warp (32 points + the zero row)
+    static constexpr int ROWS = ALIGNED ? 33 : 32;      // scratch rows per warp (+ the zero row)
     static constexpr int PATCH = ((PR * BOXC + 15) / 16) * 16;  // float2 per buffer, 128-byte multiple
     static_assert(SW + 2 * K <= G, "strip windows must fit the group");
     static_assert(kRegTile % SW == 0, "strips tile the tile");
@@ -205,7 +212,8 @@ __device__ __forceinline__ void strip_flush_init(StripFlush &fs, float *scr) {
     using S = SpreadGeo<K>;
     const int lane = threadIdx.x & 31;
     for (int i = lane; i < S::NBUF * S::PATCH; i += 32) fs.bufs[i] = make_float2(0.f, 0.f);
-    for (int i = lane; i < S::SP; i += 32) scr[32 * S::SP + i] = 0.f;
+    if constexpr (S::ALIGNED)
+        for (int i = lane; i < S::SP; i += 32) scr[32 * S::SP + i] = 0.f;
     __syncwarp();
 }
 
@@ -283,21 +291,33 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
             for (int k = 0; k < W1 / 4; ++k)
                 wq[k] = make_float4(w1[4 * k], 4 * k + 1 < W ? w1[4 * k + 1] : 0.f,
                                     4 * k + 2 < W ? w1[4 * k + 2] : 0.f, 4 * k + 3 < W ? w1[4 * k + 3] : 0.f);
-            // the group lanes' column products: zeros, then the 2K+1
-            // products at lanes q .. q+2K (q + 2K < G)
             float4 *vq = reinterpret_cast<float4 *>(sp + 4 + W1);
+            if constexpr (S::ALIGNED) {
+                // the group lanes' column products: zeros, then the 2K+1
+                // products at lanes q .. q+2K (q + 2K < G)
 #pragma unroll
-            for (int k = 0; k < S::WV / 4; ++k) vq[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-            float2 *vl = reinterpret_cast<float2 *>(sp + 4 + W1) + q;
+                for (int k = 0; k < S::WV / 4; ++k) vq[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                float2 *vl = reinterpret_cast<float2 *>(sp + 4 + W1) + q;
 #pragma unroll
-            for (int b = 0; b < W; ++b) vl[b] = make_float2(v.x * w2[b], v.y * w2[b]);
+                for (int b = 0; b < W; ++b) vl[b] = make_float2(v.x * w2[b], v.y * w2[b]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < S::WV / 4; ++k) {
+                    const float a = 2 * k < W ? w2[2 * k] : 0.f;
+                    const float b = 2 * k + 1 < W ? w2[2 * k + 1] : 0.f;
+                    vq[k] = make_float4(v.x * a, v.y * a, v.x * b, v.y * b);
+                }
+            }
         }
         if (base0 + 32 + lane < cnt) raw_next = __ldg(reinterpret_cast<const int4 *>(recs) + first + base0 + 32 + lane);
         __syncwarp();
-        // 2) operands of scratch row p for this lane: the row weights
-        //    (broadcast within the group) and this lane's column product
-        //    (row 32 is all zeros: the group has no point this step)
-        auto load = [&](int p, float (&w1)[W], float2 &vw) {
+        // 2) operands of point k + grp of the run starting at j0 for this
+        //    lane: the row weights (broadcast within the group) and this
+        //    lane's column product (zero outside the point's columns, or
+        //    when the group has no point this step)
+        auto load = [&](int j0, int k, int n, float (&w1)[W], float2 &vw) {
+            const bool ok = k + grp < n;
+            const int p = ok ? j0 + k + grp : (S::ALIGNED ? 32 : j0);
             const float *sp = scr + p * SP;
             const float4 *wq = reinterpret_cast<const float4 *>(sp + 4);
 #pragma unroll
@@ -310,7 +330,13 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
             }
 #pragma unroll
             for (int a = (W / 4) * 4; a < W; ++a) w1[a] = sp[4 + a];
-            vw = reinterpret_cast<const float2 *>(sp + 4 + W1)[gl];
+            if constexpr (S::ALIGNED) {
+                vw = reinterpret_cast<const float2 *>(sp + 4 + W1)[gl];
+            } else {
+                const int b = gl - reinterpret_cast<const int *>(sp)[1];
+                vw = (ok && static_cast<unsigned>(b) < static_cast<unsigned>(W))
+                         ? reinterpret_cast<const float2 *>(sp + 4 + W1)[b] : make_float2(0.f, 0.f);
+            }
         };
         // The binning keeps a work item's keys ascending; a batch out of
         // order can only follow a record that failed the bounds check above
@@ -346,7 +372,7 @@ __device__ __forceinline__ void spread_item(const Rec32 *__restrict__ recs, int 
                     for (int k = 0; k < n; k += S::NG) {
                         float w1[W];
                         float2 vw;
-                        load(k + grp < n ? j + k + grp : 32, w1, vw);
+                        load(j, k, n, w1, vw);
                         add_rows2<K, PR, L>(acc, w1, vw);
                     }
                     j += n;

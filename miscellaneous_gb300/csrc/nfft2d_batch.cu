@@ -312,7 +312,7 @@ void batch_free(nfft2d_batch_s *b) {
     for (auto &gx : b->graph)
         if (gx) cudaGraphExecDestroy(gx);
     for (auto &gr : b->groups)
-        if (gr.fft_ok) cufftDestroy(gr.fft);
+        if (gr.fft_ok) pooled_plan_release(gr.fft);
     for (auto *p : b->plans) release_plan(p);
     cudaFree(b->grids);
     cudaFree(b->d_desc);
@@ -583,8 +583,8 @@ int nfft2d_batch_create_k(nfft2d_batch *out, int count, const int *N1, const int
         const Geom &g = b->plans[gr.members[0]]->g;
         int nn[2] = {g.n1, g.n2}, emb[2] = {g.Ra, g.C};
         const int dist = g.Ra * g.C;
-        if (cufftPlanMany(&gr.fft, 2, nn, emb, 1, dist, emb, 1, dist, CUFFT_C2C,
-                          static_cast<int>(gr.members.size())) != CUFFT_SUCCESS)
+        if (pooled_plan_many(&gr.fft, 2, nn, emb, 1, dist, emb, 1, dist, CUFFT_C2C,
+                             static_cast<int>(gr.members.size())) != CUFFT_SUCCESS)
             return fail(NFFT2D_ERR_CUFFT);
         gr.fft_ok = true;
         if (cufftSetStream(gr.fft, b->stream) != CUFFT_SUCCESS) return fail(NFFT2D_ERR_CUFFT);

@@ -487,8 +487,9 @@ bool fused_fft_eligible(int precision, int n1, int n2) {
 }
 
 int setup_fused_fft(nfft2d_plan_s *p) {
-    cudaFree(p->tw1);
-    cudaFree(p->tw2);
+    if (p->tw1 || p->tw2) cudaStreamSynchronize(p->stream);  // no transform on the old tables in flight
+    plan_free(p->tw1);
+    plan_free(p->tw2);
     p->tw1 = p->tw2 = nullptr;
     p->fused_ok = false;
     if (!fused_fft_eligible(p->precision, p->g.n1, p->g.n2)) return NFFT2D_OK;

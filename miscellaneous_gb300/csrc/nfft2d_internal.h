@@ -191,6 +191,20 @@ int tensor_map_for(nfft2d_plan_s *p);
 int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype, double u1,
                       double u2, double o1, double o2, bool async = false);
 
+// cuFFT plans from a process-wide pool keyed by the device and every plan
+// parameter: creating a plan of an awkward size costs milliseconds (a
+// Bluestein length: 1.4 ms at 98 x 485, 6 ms at 552 x 970 on GB300), and
+// callers that build and drop plans of recurring shapes (the FFBP
+// recursion's regriddings, repeated type-3 calls, batches) take a released
+// one back instead.  A handle is owned by one caller between acquire and
+// release (cuFFT plans are not shareable between concurrent executions);
+// released handles are kept up to 256 plans / 1 GiB of work area, oldest
+// destroyed first.  inembed/onembed may be NULL (the basic layout).
+cufftResult pooled_plan_many(cufftHandle *out, int rank, const int *n, const int *inembed, int istride, int idist,
+                             const int *onembed, int ostride, int odist, cufftType type, int batch);
+cufftResult pooled_plan_2d(cufftHandle *out, int nx, int ny, cufftType type);
+void pooled_plan_release(cufftHandle h);
+
 // After the plan's status words were copied to p->h_status and its stream
 // went idle: completes a set_points enqueued by nfft2d_set_points_async
 // (the work-item count) and reports, then clears, the latched device-side
@@ -205,10 +219,15 @@ int apply_status(nfft2d_plan_s *p);
 typedef cudaError_t (*PadFn)(const nfft2d_plan_s *p, const void *ctx);
 int type2_with_pad(nfft2d_plan_s *p, int sign, void *f, PadFn pad, const void *ctx);
 
-// cudaMalloc / cudaMallocHost for plan buffers, with the host-side
-// allocation-failure hook used by the tests (NFFT2D_FAIL_ALLOC_AT).
+// Device and page-locked allocations of plan buffers (cached, see
+// nfft2d_plan.cu), with the host-side allocation-failure hook used by the
+// tests (NFFT2D_FAIL_ALLOC_AT).
 cudaError_t plan_malloc(void **ptr, size_t bytes);
 cudaError_t plan_malloc_host(void **ptr, size_t bytes);
+void plan_free_host(void *ptr, size_t bytes);  // the counterpart of plan_malloc_host (same size)
+// The counterpart of plan_malloc: the block goes back to the cache (the
+// caller has no work on it in flight).  Any other device pointer is freed.
+void plan_free(void *ptr);
 
 // The fused FFT passes (nfft2d_fft.cu): eligibility, per-plan twiddle tables,
 // type 2 = deapodize/pad + band-column FFT, then row FFT + halo fill;

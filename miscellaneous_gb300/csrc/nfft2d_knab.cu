@@ -318,27 +318,35 @@ namespace {
 
 void knab_free(nfft2d_knab_s *k) {
     if (!k) return;
+    // nothing of the regridder in flight: its FFT handle and buffers go back
+    // to the library's caches
+    cudaStreamSynchronize(k->stream);
     if (k->plan) release_plan(k->plan);
-    if (k->fft_ok) cufftDestroy(k->raster_fft);
-    cudaFree(k->spec);
-    cudaFree(k->d_partial);
-    cudaFree(k->d_count);
-    cudaFree(k->wrow);
-    cudaFree(k->wcol);
-    cudaFree(k->row_mask);
-    cudaFree(k->col_mask);
+    if (k->fft_ok) pooled_plan_release(k->raster_fft);
+    plan_free(k->spec);
+    plan_free(k->d_partial);
+    plan_free(k->d_count);
+    plan_free(k->wrow);
+    plan_free(k->wcol);
+    plan_free(k->row_mask);
+    plan_free(k->col_mask);
     delete k;
 }
 
 size_t real_bytes(int precision) { return precision == NFFT2D_F64 ? sizeof(double) : sizeof(float); }
 size_t cplx_bytes(int precision) { return 2 * real_bytes(precision); }
 
-int ensure_bytes(void **ptr, size_t *cap, size_t need) {
+// A device buffer of at least `need` bytes; a smaller one goes back to the
+// cache once the stream's work on it is done.
+int ensure_bytes(void **ptr, size_t *cap, size_t need, cudaStream_t st) {
     if (*cap >= need && *ptr) return NFFT2D_OK;
-    cudaFree(*ptr);
+    if (*ptr) {
+        cudaStreamSynchronize(st);
+        plan_free(*ptr);
+    }
     *ptr = nullptr;
     *cap = 0;
-    KNAB_TRY_CUDA(cudaMalloc(ptr, need));
+    KNAB_TRY_CUDA(plan_malloc(ptr, need));
     *cap = need;
     return NFFT2D_OK;
 }
@@ -372,9 +380,9 @@ int upload_weights(nfft2d_knab_s *k) {
     for (long j = 0; j < nr; ++j) wr[j] = k->Gm[j] * d1[(j - k->kgm) + N1 / 2];
     for (long j = 0; j < nc; ++j) wc[j] = k->Gn[j] * d2[(j - k->kgn) + N2 / 2];
     const size_t rb = real_bytes(k->precision);
-    int st = ensure_bytes(&k->wrow, &k->wrow_cap, rb * nr);
+    int st = ensure_bytes(&k->wrow, &k->wrow_cap, rb * nr, k->stream);
     if (st != NFFT2D_OK) return st;
-    if ((st = ensure_bytes(&k->wcol, &k->wcol_cap, rb * nc)) != NFFT2D_OK) return st;
+    if ((st = ensure_bytes(&k->wcol, &k->wcol_cap, rb * nc, k->stream)) != NFFT2D_OK) return st;
     if (k->precision == NFFT2D_F64) {
         KNAB_TRY_CUDA(cudaMemcpy(k->wrow, wr.data(), rb * nr, cudaMemcpyHostToDevice));
         KNAB_TRY_CUDA(cudaMemcpy(k->wcol, wc.data(), rb * nc, cudaMemcpyHostToDevice));
@@ -474,13 +482,14 @@ int nfft2d_knab_create(nfft2d_knab *out, int Nrows, int Ncols, const double *rho
     if (cudaDeviceGetAttribute(&k->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return fail(NFFT2D_ERR_CUDA);
     const cufftType t = precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C;
-    if (cufftPlan2d(&k->raster_fft, Nrows, Ncols, t) != CUFFT_SUCCESS) return fail(NFFT2D_ERR_CUFFT);
+    if (pooled_plan_2d(&k->raster_fft, Nrows, Ncols, t) != CUFFT_SUCCESS) return fail(NFFT2D_ERR_CUFFT);
     k->fft_ok = true;
     if (cufftSetStream(k->raster_fft, k->stream) != CUFFT_SUCCESS) return fail(NFFT2D_ERR_CUFFT);
-    if (cudaMalloc(&k->spec, cplx_bytes(precision) * static_cast<size_t>(Nrows) * Ncols) != cudaSuccess)
+    if (plan_malloc(&k->spec, cplx_bytes(precision) * static_cast<size_t>(Nrows) * Ncols) != cudaSuccess)
         return fail(NFFT2D_ERR_OOM);
-    if (cudaMalloc(&k->d_partial, sizeof(double) * 4 * kMinmaxBlocks) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
-    if (cudaMalloc(&k->d_count, 2 * sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
+    if (plan_malloc(reinterpret_cast<void **>(&k->d_partial), sizeof(double) * 4 * kMinmaxBlocks) != cudaSuccess)
+        return fail(NFFT2D_ERR_OOM);
+    if (plan_malloc(reinterpret_cast<void **>(&k->d_count), 2 * sizeof(int)) != cudaSuccess) return fail(NFFT2D_ERR_OOM);
     *out = k;
     return NFFT2D_OK;
 }
@@ -506,12 +515,12 @@ int nfft2d_knab_set_points(nfft2d_knab k, int len1, int len2, const void *rho_ou
     {
         void *p = k->row_mask;
         size_t cap = static_cast<size_t>(k->row_cap);
-        if ((st = ensure_bytes(&p, &cap, static_cast<size_t>(len1))) != NFFT2D_OK) return st;
+        if ((st = ensure_bytes(&p, &cap, static_cast<size_t>(len1), k->stream)) != NFFT2D_OK) return st;
         k->row_mask = static_cast<unsigned char *>(p);
         k->row_cap = static_cast<int>(cap);
         p = k->col_mask;
         cap = static_cast<size_t>(k->col_cap);
-        if ((st = ensure_bytes(&p, &cap, static_cast<size_t>(len2))) != NFFT2D_OK) return st;
+        if ((st = ensure_bytes(&p, &cap, static_cast<size_t>(len2), k->stream)) != NFFT2D_OK) return st;
         k->col_mask = static_cast<unsigned char *>(p);
         k->col_cap = static_cast<int>(cap);
     }

@@ -110,6 +110,37 @@ double nfft2d::fit_window_poly(double sigma, int K, WinPoly *out) {
     return maxerr;
 }
 
+namespace {
+// The fitted window of every (sigma, K) a process has used: plans of the same
+// window (every regridding of an FFBP image, every transform of a batch)
+// share one fit instead of refitting on each plan creation.
+struct PolyCacheEntry {
+    double sigma;
+    int K;
+    double err;
+    nfft2d::WinPoly poly;
+};
+std::mutex g_poly_mu;
+std::vector<PolyCacheEntry> g_poly_cache;
+
+double cached_window_poly(double sigma, int K, nfft2d::WinPoly *out) {
+    {
+        std::lock_guard<std::mutex> lock(g_poly_mu);
+        for (const auto &e : g_poly_cache)
+            if (e.sigma == sigma && e.K == K) {
+                *out = e.poly;
+                return e.err;
+            }
+    }
+    const double err = nfft2d::fit_window_poly(sigma, K, out);
+    if (err >= 0.0) {
+        std::lock_guard<std::mutex> lock(g_poly_mu);
+        if (g_poly_cache.size() < 64) g_poly_cache.push_back({sigma, K, err, *out});
+    }
+    return err;
+}
+}  // namespace
+
 // Device allocations of a plan.  For tests of the host-side failure paths,
 // NFFT2D_FAIL_ALLOC_AT=k makes the k-th allocation (counted from the moment
 // the variable takes that value) report cudaErrorMemoryAllocation without
@@ -131,20 +162,134 @@ static bool injected_alloc_failure() {
     return ++count == std::atoll(v);
 }
 
+// Plan buffers come from a process-wide cache of freed device blocks: a
+// cudaMalloc / cudaFree pair costs ~0.06-0.09 ms on GB300 and cudaFree waits
+// for the whole device, while callers that make and drop plans (the FFBP
+// recursion: two plans and a regridder per node) reuse the same sizes.  A
+// request takes the smallest cached block of at least its size and at most
+// twice it; freed blocks are kept up to 1 GiB, the oldest released first.
+// Callers return a block only once no work of theirs that uses it is in
+// flight (they synchronize the stream first).
+namespace {
+constexpr size_t kBlockCacheBytes = size_t(1) << 30;
+struct CachedBlock {
+    void *p;
+    size_t bytes;
+    unsigned long long age;
+};
+std::mutex g_blk_mu;
+std::vector<CachedBlock> g_blk_free;
+std::vector<std::pair<void *, size_t>> g_blk_live;
+size_t g_blk_free_bytes = 0;
+unsigned long long g_blk_clock = 0;
+int g_blk_device = -1;
+}  // namespace
+
 cudaError_t nfft2d::plan_malloc(void **ptr, size_t bytes) {
     if (injected_alloc_failure()) {
         *ptr = nullptr;
         return cudaErrorMemoryAllocation;
     }
-    return cudaMalloc(ptr, bytes);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lock(g_blk_mu);
+        if (g_blk_device == dev) {
+            size_t best = g_blk_free.size();
+            for (size_t i = 0; i < g_blk_free.size(); ++i)
+                if (g_blk_free[i].bytes >= bytes && g_blk_free[i].bytes <= 2 * bytes + 4096 &&
+                    (best == g_blk_free.size() || g_blk_free[i].bytes < g_blk_free[best].bytes))
+                    best = i;
+            if (best < g_blk_free.size()) {
+                const CachedBlock b = g_blk_free[best];
+                g_blk_free.erase(g_blk_free.begin() + static_cast<long>(best));
+                g_blk_free_bytes -= b.bytes;
+                g_blk_live.push_back({b.p, b.bytes});
+                *ptr = b.p;
+                return cudaSuccess;
+            }
+        }
+    }
+    const cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(g_blk_mu);
+    if (g_blk_device != dev) {  // blocks belong to one device: start over on another
+        for (const auto &b : g_blk_free) cudaFree(b.p);
+        g_blk_free.clear();
+        g_blk_free_bytes = 0;
+        g_blk_device = dev;
+    }
+    g_blk_live.push_back({*ptr, bytes});
+    return cudaSuccess;
 }
+
+void nfft2d::plan_free(void *ptr) {
+    if (!ptr) return;
+    std::vector<void *> drop;
+    {
+        std::lock_guard<std::mutex> lock(g_blk_mu);
+        size_t i = 0;
+        while (i < g_blk_live.size() && g_blk_live[i].first != ptr) ++i;
+        if (i == g_blk_live.size()) {
+            drop.push_back(ptr);  // not from plan_malloc
+        } else {
+            const size_t bytes = g_blk_live[i].second;
+            g_blk_live.erase(g_blk_live.begin() + static_cast<long>(i));
+            g_blk_free.push_back({ptr, bytes, ++g_blk_clock});
+            g_blk_free_bytes += bytes;
+            while (g_blk_free_bytes > kBlockCacheBytes && !g_blk_free.empty()) {
+                size_t old = 0;
+                for (size_t j = 1; j < g_blk_free.size(); ++j)
+                    if (g_blk_free[j].age < g_blk_free[old].age) old = j;
+                drop.push_back(g_blk_free[old].p);
+                g_blk_free_bytes -= g_blk_free[old].bytes;
+                g_blk_free.erase(g_blk_free.begin() + static_cast<long>(old));
+            }
+        }
+    }
+    for (void *d : drop) cudaFree(d);
+}
+
+// Page-locked status words: 16-byte slots cut from 4 KB page-locked blocks
+// that live as long as the process (a page-locked allocation costs ~0.25 ms
+// on GB300; plans that come and go -- the FFBP recursion makes over a
+// hundred per image -- take a slot instead).  Requests above one slot are
+// plain page-locked allocations.
+namespace {
+constexpr size_t kSlotBytes = 16, kSlotBlock = 4096;
+std::mutex g_slot_mu;
+std::vector<void *> g_slot_free;
+}  // namespace
 
 cudaError_t nfft2d::plan_malloc_host(void **ptr, size_t bytes) {
     if (injected_alloc_failure()) {
         *ptr = nullptr;
         return cudaErrorMemoryAllocation;
     }
-    return cudaMallocHost(ptr, bytes);
+    if (bytes > kSlotBytes) return cudaMallocHost(ptr, bytes);
+    std::lock_guard<std::mutex> lock(g_slot_mu);
+    if (g_slot_free.empty()) {
+        void *blk = nullptr;
+        const cudaError_t e = cudaMallocHost(&blk, kSlotBlock);
+        if (e != cudaSuccess) {
+            *ptr = nullptr;
+            return e;
+        }
+        for (size_t o = 0; o < kSlotBlock; o += kSlotBytes) g_slot_free.push_back(static_cast<char *>(blk) + o);
+    }
+    *ptr = g_slot_free.back();
+    g_slot_free.pop_back();
+    return cudaSuccess;
+}
+
+void nfft2d::plan_free_host(void *ptr, size_t bytes) {
+    if (!ptr) return;
+    if (bytes > kSlotBytes) {
+        cudaFreeHost(ptr);
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_slot_mu);
+    g_slot_free.push_back(ptr);
 }
 
 namespace {
@@ -714,11 +859,13 @@ __global__ void __launch_bounds__(kItemScanThreads, 1) k_scan_emit_chunks(const 
 // plan helpers
 // ---------------------------------------------------------------------------
 void free_points(nfft2d_plan_s *p) {
-    cudaFree(p->recs);
-    cudaFree(p->tmp_recs);
-    cudaFree(p->keyrank);
-    cudaFree(p->src);
-    cudaFree(p->chunks);
+    if (p->recs || p->tmp_recs || p->keyrank || p->src || p->chunks)
+        cudaStreamSynchronize(p->stream);  // no transform of the old points in flight
+    plan_free(p->recs);
+    plan_free(p->tmp_recs);
+    plan_free(p->keyrank);
+    plan_free(p->src);
+    plan_free(p->chunks);
     p->recs = p->tmp_recs = nullptr;
     p->keyrank = nullptr;
     p->src = nullptr;
@@ -727,23 +874,33 @@ void free_points(nfft2d_plan_s *p) {
     p->chunks_cap = 0;
 }
 
+// The plan's cuFFT handles back to the pool, once no transform of the plan
+// is in flight (another stream may take a handle, and its work area, next).
+void release_ffts(nfft2d_plan_s *p) {
+    if (!p->fft_ok && !p->pruned_ok) return;
+    cudaStreamSynchronize(p->stream);
+    if (p->fft_ok) pooled_plan_release(p->fft);
+    if (p->pruned_ok) {
+        pooled_plan_release(p->fft_rows);
+        pooled_plan_release(p->fft_cols);
+    }
+    p->fft_ok = p->pruned_ok = false;
+}
+
 void destroy_plan(nfft2d_plan_s *p) {
     if (!p) return;
-    if (p->fft_ok) cufftDestroy(p->fft);
-    if (p->pruned_ok) {
-        cufftDestroy(p->fft_rows);
-        cufftDestroy(p->fft_cols);
-    }
+    cudaStreamSynchronize(p->stream);  // its buffers go back to the cache: nothing of the plan in flight
+    release_ffts(p);
     free_points(p);
-    if (!p->grid_external) cudaFree(p->grid);
-    cudaFree(p->deap1);
-    cudaFree(p->deap2);
-    cudaFree(p->d_status);
-    cudaFreeHost(p->h_status);
-    cudaFree(p->tw1);
-    cudaFree(p->tw2);
-    cudaFree(p->cell_count);
-    cudaFree(p->scan_tmp);
+    if (!p->grid_external) plan_free(p->grid);
+    plan_free(p->deap1);
+    plan_free(p->deap2);
+    plan_free(p->d_status);
+    plan_free_host(p->h_status, 4 * sizeof(int));
+    plan_free(p->tw1);
+    plan_free(p->tw2);
+    plan_free(p->cell_count);
+    plan_free(p->scan_tmp);
     for (auto &e : p->timer.ev)
         if (e) cudaEventDestroy(e);
     delete p;
@@ -780,57 +937,65 @@ size_t plan_workspace_bytes(const nfft2d_plan_s *p) {
 
 int check_plan(nfft2d_plan_s *p) { return p ? NFFT2D_OK : NFFT2D_ERR_INVALID_ARG; }
 
-// (Re)allocate the padded grid for the current geometry, rebuild the cuFFT
-// plan on its interior (advanced layout) and the TMA descriptor.
+// The cuFFT plans on the padded grid's interior (advanced layout) that the
+// plan's FFT mode runs on, taken from the pool when missing: the 2D plan, or
+// from 2048 x 2048 cells up (or fft_mode 1) the pruned pair -- n1 rows of n2
+// points (contiguous, pitch C) and N2/2 columns of n1 points (stride C), run
+// once per half of the band -- with the 2D plan as the fallback.  Nothing
+// for the fused passes.  Plans for a batch's external grid are the batch's.
+int ensure_ffts(nfft2d_plan_s *p) {
+    if (p->grid_external || use_fused(p)) return NFFT2D_OK;
+    const Geom &g = p->g;
+    const cufftType t = p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C;
+    const bool pruned = p->fft_mode == 1 || (p->fft_mode < 0 && 1LL * g.n1 * g.n2 >= 2048LL * 2048LL);
+    if (pruned && !p->pruned_ok) {
+        const int nr[1] = {g.n2}, er[1] = {g.C};
+        const int nc[1] = {g.n1}, ec[1] = {g.Ra};
+        if (pooled_plan_many(&p->fft_rows, 1, nr, er, 1, g.C, er, 1, g.C, t, g.n1) == CUFFT_SUCCESS) {
+            if (pooled_plan_many(&p->fft_cols, 1, nc, ec, g.C, 1, ec, g.C, 1, t, p->N2 / 2) == CUFFT_SUCCESS) {
+                p->pruned_ok = cufftSetStream(p->fft_rows, p->stream) == CUFFT_SUCCESS &&
+                               cufftSetStream(p->fft_cols, p->stream) == CUFFT_SUCCESS;
+                if (!p->pruned_ok) {
+                    pooled_plan_release(p->fft_rows);
+                    pooled_plan_release(p->fft_cols);
+                }
+            } else {
+                pooled_plan_release(p->fft_rows);
+            }
+        }
+    }
+    if ((!pruned || !p->pruned_ok) && !p->fft_ok) {
+        const int n[2] = {g.n1, g.n2};
+        const int emb[2] = {g.Ra, g.C};
+        const int dist = g.Ra * g.C;
+        cufftResult fr = pooled_plan_many(&p->fft, 2, n, emb, 1, dist, emb, 1, dist, t, 1);
+        if (fr != CUFFT_SUCCESS) return status_from_cufft(fr);
+        p->fft_ok = true;
+        if ((fr = cufftSetStream(p->fft, p->stream)) != CUFFT_SUCCESS) return status_from_cufft(fr);
+    }
+    return NFFT2D_OK;
+}
+
+// (Re)allocate the padded grid for the current geometry, take the cuFFT
+// plans its FFT mode needs and rebuild the TMA descriptor.
 int setup_grid(nfft2d_plan_s *p) {
     const Geom &g = p->g;
-    if (p->fft_ok) {
-        cufftDestroy(p->fft);
-        p->fft_ok = false;
-    }
-    if (p->pruned_ok) {
-        cufftDestroy(p->fft_rows);
-        cufftDestroy(p->fft_cols);
-        p->pruned_ok = false;
-    }
+    release_ffts(p);
     p->tmap_ok = false;
     if (!p->grid_external) {
-        cudaFree(p->grid);
+        if (p->grid) cudaStreamSynchronize(p->stream);  // no transform on the old grid in flight
+        plan_free(p->grid);
         p->grid = nullptr;
         // 256 zeroed bytes of slack after the grid: the 16-byte-load gather
         // may read one complex past the last row's end (with weight 0)
         const size_t bytes = cplx_size(p->precision) * static_cast<size_t>(g.Ra) * g.C + 256;
         NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->grid), bytes));
         NFFT_TRY_CUDA(cudaMemsetAsync(p->grid, 0, bytes, p->stream));
-        int n[2] = {g.n1, g.n2};
-        int emb[2] = {g.Ra, g.C};
-        const int dist = g.Ra * g.C;
-        cufftResult fr = cufftPlanMany(&p->fft, 2, n, emb, 1, dist, emb, 1, dist,
-                                       p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C, 1);
-        if (fr != CUFFT_SUCCESS) return status_from_cufft(fr);
-        p->fft_ok = true;
-        if ((fr = cufftSetStream(p->fft, p->stream)) != CUFFT_SUCCESS) return status_from_cufft(fr);
-        // the pruned pair: n1 rows of n2 points (contiguous, pitch C), and
-        // N2/2 columns of n1 points (stride C) run once per half of the band
-        const cufftType t = p->precision == NFFT2D_F64 ? CUFFT_Z2Z : CUFFT_C2C;
-        int nr[1] = {g.n2}, er[1] = {g.C};
-        int nc[1] = {g.n1}, ec[1] = {g.Ra};
-        if (cufftPlanMany(&p->fft_rows, 1, nr, er, 1, g.C, er, 1, g.C, t, g.n1) == CUFFT_SUCCESS) {
-            if (cufftPlanMany(&p->fft_cols, 1, nc, ec, g.C, 1, ec, g.C, 1, t, p->N2 / 2) == CUFFT_SUCCESS) {
-                p->pruned_ok = cufftSetStream(p->fft_rows, p->stream) == CUFFT_SUCCESS &&
-                               cufftSetStream(p->fft_cols, p->stream) == CUFFT_SUCCESS;
-                if (!p->pruned_ok) {
-                    cufftDestroy(p->fft_rows);
-                    cufftDestroy(p->fft_cols);
-                }
-            } else {
-                cufftDestroy(p->fft_rows);
-            }
-        }
-    }
-    if (!p->grid_external) {
         const int st = setup_fused_fft(p);
         if (st != NFFT2D_OK) return st;
+        // the cuFFT plans the current FFT mode runs on (none for the fused passes)
+        const int sf = ensure_ffts(p);
+        if (sf != NFFT2D_OK) return sf;
     }
     if (p->precision == NFFT2D_F32) return make_tensor_map(p);
     return NFFT2D_OK;
@@ -839,8 +1004,9 @@ int setup_grid(nfft2d_plan_s *p) {
 // (Re)allocate the bin counters for the current tile geometry.
 int setup_bins(nfft2d_plan_s *p) {
     const Geom &g = p->g;
-    cudaFree(p->cell_count);
-    cudaFree(p->scan_tmp);
+    if (p->cell_count || p->scan_tmp) cudaStreamSynchronize(p->stream);
+    plan_free(p->cell_count);
+    plan_free(p->scan_tmp);
     p->cell_count = p->scan_tmp = nullptr;
     p->ncells = static_cast<size_t>(g.tiles1) * g.tiles2 * g.T * g.T;
     const size_t ntiles = static_cast<size_t>(g.tiles1) * g.tiles2;
@@ -1040,6 +1206,10 @@ int run_fft(nfft2d_plan_s *p, int sign, bool type2) {
     // below that cuFFT's single 2D plan is faster on GB300 (1024^2: 20 us
     // vs 30 us; 2048^2: 40 vs 35 us; 4096^2: 153 vs 112 us)
     const bool pruned = p->fft_mode == 1 || (p->fft_mode < 0 && 1LL * g.n1 * g.n2 >= 2048LL * 2048LL);
+    if (!(pruned && p->pruned_ok) && !p->fft_ok) {  // a mode set on a plan made without its plans
+        const int st = ensure_ffts(p);
+        if (st != NFFT2D_OK) return st;
+    }
     if (!(pruned && p->pruned_ok)) return status_from_cufft(exec_at(p, p->fft, off, dir));
     const size_t right = off + static_cast<size_t>(g.n2 - p->N2 / 2);  // first column of the negative band
     cufftResult r;
@@ -1186,7 +1356,7 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     p->w.alpha = alpha;
     p->w.cn = K / std::sinh(alpha * K);
     p->w.kp = K / (1.0 - std::exp(-2.0 * alpha * K));
-    const double poly_err = fit_window_poly(sigma, K, &p->poly);
+    const double poly_err = cached_window_poly(sigma, K, &p->poly);
     if (!(poly_err >= 0.0 && poly_err < 1e-8)) return fail(NFFT2D_ERR_INTERNAL);
 
     const size_t rs = real_size(precision);
@@ -1218,8 +1388,7 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
         if (e != cudaSuccess) return fail(status_from_cuda(e));
     }
 
-    for (auto &ev : p->timer.ev)
-        if (cudaEventCreate(&ev) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
+    // the stage events are created when timing is first enabled
     if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return fail(status_from_cuda(e));
     p->workspace_bytes = plan_workspace_bytes(p);
     *out = p;
@@ -1253,7 +1422,7 @@ int nfft2d_set_stream(nfft2d_plan p, void *stream) {
         if (r == CUFFT_SUCCESS) r = cufftSetStream(p->fft_cols, p->stream);
         if (r != CUFFT_SUCCESS) return status_from_cufft(r);
     }
-    return status_from_cufft(cufftSetStream(p->fft, p->stream));
+    return p->fft_ok ? status_from_cufft(cufftSetStream(p->fft, p->stream)) : NFFT2D_OK;
 }
 
 int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
@@ -1297,7 +1466,11 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     }
     if (t->fft_mode > 2 || t->fft_mode < -1) return NFFT2D_ERR_INVALID_ARG;
     if (t->fft_mode == 2 && !p->fused_ok) return NFFT2D_ERR_UNSUPPORTED;
-    if (t->fft_mode >= 0) p->fft_mode = t->fft_mode;
+    if (t->fft_mode >= 0) {
+        p->fft_mode = t->fft_mode;
+        const int sf = ensure_ffts(p);  // the new mode's cuFFT plans now, not inside a transform
+        if (sf != NFFT2D_OK) return sf;
+    }
     p->workspace_bytes = plan_workspace_bytes(p);
     return NFFT2D_OK;
 }
@@ -1654,6 +1827,9 @@ int nfft2d_plan_selftest_wait_timeout(nfft2d_plan p, int spin_limit) {
 
 int nfft2d_enable_timing(nfft2d_plan p, int on) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
+    if (on)
+        for (auto &ev : p->timer.ev)
+            if (!ev) NFFT_TRY_CUDA(cudaEventCreate(&ev));
     p->timer.on = on != 0;
     for (bool &u : p->timer.used) u = false;
     return NFFT2D_OK;
@@ -1676,3 +1852,107 @@ int nfft2d_get_timings(nfft2d_plan p, nfft2d_timings *t) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// cuFFT plan pool
+// ---------------------------------------------------------------------------
+namespace {
+struct FftKey {
+    int v[20];
+    bool operator==(const FftKey &o) const { return std::memcmp(v, o.v, sizeof v) == 0; }
+};
+struct FftEntry {
+    FftKey key;
+    cufftHandle h;
+    size_t bytes;
+};
+constexpr size_t kFftPoolPlans = 256;
+constexpr size_t kFftPoolBytes = size_t(1) << 30;
+std::mutex g_fft_mu;
+std::vector<FftEntry> g_fft_free;  // released plans, oldest first
+std::vector<FftEntry> g_fft_live;  // plans handed out
+size_t g_fft_free_bytes = 0;
+
+FftKey fft_key(int rank, const int *n, const int *inembed, int istride, int idist, const int *onembed, int ostride,
+               int odist, cufftType type, int batch) {
+    FftKey k;
+    std::memset(k.v, 0, sizeof k.v);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    k.v[0] = dev;
+    k.v[1] = rank;
+    k.v[2] = static_cast<int>(type);
+    k.v[3] = batch;
+    k.v[4] = inembed ? 1 : 0;
+    k.v[5] = onembed ? 1 : 0;
+    k.v[6] = istride;
+    k.v[7] = idist;
+    k.v[8] = ostride;
+    k.v[9] = odist;
+    for (int d = 0; d < rank && d < 3; ++d) {
+        k.v[10 + d] = n[d];
+        k.v[13 + d] = inembed ? inembed[d] : 0;
+        k.v[16 + d] = onembed ? onembed[d] : 0;
+    }
+    return k;
+}
+}  // namespace
+
+cufftResult nfft2d::pooled_plan_many(cufftHandle *out, int rank, const int *n, const int *inembed, int istride,
+                                     int idist, const int *onembed, int ostride, int odist, cufftType type,
+                                     int batch) {
+    if (rank < 1 || rank > 3) return CUFFT_INVALID_VALUE;
+    const FftKey key = fft_key(rank, n, inembed, istride, idist, onembed, ostride, odist, type, batch);
+    {
+        std::lock_guard<std::mutex> lock(g_fft_mu);
+        for (size_t i = g_fft_free.size(); i-- > 0;)
+            if (g_fft_free[i].key == key) {
+                const FftEntry e = g_fft_free[i];
+                g_fft_free.erase(g_fft_free.begin() + static_cast<long>(i));
+                g_fft_free_bytes -= e.bytes;
+                g_fft_live.push_back(e);
+                *out = e.h;
+                return CUFFT_SUCCESS;
+            }
+    }
+    cufftHandle h;
+    cufftResult r = cufftPlanMany(&h, rank, const_cast<int *>(n), const_cast<int *>(inembed), istride, idist,
+                                  const_cast<int *>(onembed), ostride, odist, type, batch);
+    if (r != CUFFT_SUCCESS) return r;
+    size_t bytes = 0;
+    if (cufftGetSize(h, &bytes) != CUFFT_SUCCESS) bytes = 0;
+    std::lock_guard<std::mutex> lock(g_fft_mu);
+    g_fft_live.push_back({key, h, bytes});
+    *out = h;
+    return CUFFT_SUCCESS;
+}
+
+cufftResult nfft2d::pooled_plan_2d(cufftHandle *out, int nx, int ny, cufftType type) {
+    const int n[2] = {nx, ny};
+    return pooled_plan_many(out, 2, n, nullptr, 1, 0, nullptr, 1, 0, type, 1);
+}
+
+void nfft2d::pooled_plan_release(cufftHandle h) {
+    std::vector<cufftHandle> drop;
+    {
+        std::lock_guard<std::mutex> lock(g_fft_mu);
+        size_t i = 0;
+        while (i < g_fft_live.size() && g_fft_live[i].h != h) ++i;
+        if (i == g_fft_live.size()) {
+            drop.push_back(h);  // not from the pool
+        } else {
+            const FftEntry e = g_fft_live[i];
+            g_fft_live.erase(g_fft_live.begin() + static_cast<long>(i));
+            g_fft_free.push_back(e);
+            g_fft_free_bytes += e.bytes;
+            while (!g_fft_free.empty() &&
+                   (g_fft_free.size() > kFftPoolPlans || g_fft_free_bytes > kFftPoolBytes)) {
+                drop.push_back(g_fft_free.front().h);
+                g_fft_free_bytes -= g_fft_free.front().bytes;
+                g_fft_free.erase(g_fft_free.begin());
+            }
+        }
+    }
+    for (cufftHandle d : drop) cufftDestroy(d);
+}
+

@@ -13,11 +13,15 @@
 // The reference's circular shift by half the grid with the (-1)^(i+j)
 // checkerboard (:135-151) is folded into the gather's indexing: no pass.
 //
-// Kernels: one warp per input point for the spread (lanes walk the columns
-// of the (2 msp + 1)^2 footprint, so each row's atomic adds are contiguous)
-// and one warp per output frequency for the gather (the same footprint,
-// coalesced row reads, a warp-shuffle reduction).  Weights and coordinates
-// are FP64; the grid and the sums use the data precision.
+// Kernels: the Gaussian weight of a footprint tap factors into a row and a
+// column weight, so a point or frequency needs 2(2 msp + 1) exponentials
+// (FP64, from FP64 coordinates), not (2 msp + 1)^2.  The spread bins the
+// points by 16 x 16 grid tile and accumulates each tile's points in a
+// shared-memory patch (warps own disjoint patch rows: no atomics) that one
+// global atomic add per cell puts into the grid; the gather runs one warp
+// per output frequency over the footprint with coalesced row reads and a
+// warp-shuffle reduction.  The grid, the products and the sums use the
+// data precision.
 #include <cuda_runtime.h>
 #include <cufft.h>
 
@@ -81,74 +85,323 @@ __device__ __forceinline__ int wrap(long long i, int n) {
     return static_cast<int>(r < 0 ? r + n : r);
 }
 
-template <typename C2, typename Real>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    k_t3_spread(const double *__restrict__ x, const double *__restrict__ y, const C2 *__restrict__ f, long long n,
-                Params P, C2 *__restrict__ grid) {
-    const long long p = blockIdx.x * static_cast<long long>(kWarpsPerBlock) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
+// ---------------------------------------------------------------------------
+// Spreading (NFFT3_2D_C.cpp:38-85), binned.  Tap (r, c) of a point has the
+// weight exp(ex(c) + ey(r)) with ex depending on the column only and ey on
+// the row only (:61-74), so a point needs 2(2ms+1) exponentials, not
+// (2ms+1)^2, and the products wr(r) wc(c) are formed in the data precision.
+// Points are binned by the TS x TS grid tile of their footprint's first
+// cell; a CTA accumulates one work item (at most kT3Item points of one
+// tile) into a shared-memory patch of (TS + W - 1)^2 cells -- warp w owns
+// the patch rows r = w (mod 8), so no two threads ever touch one cell and no
+// shared atomics are needed -- and adds the patch into the grid with one
+// global atomic add per cell and component.
+// ---------------------------------------------------------------------------
+constexpr int kT3Tile = 16;    // TS
+constexpr int kT3Item = 1024;  // points per work item
+constexpr int kT3Warps = 8;    // warps of a spreading CTA
+
+struct T3Rec {
+    double xt, yt;  // (x - xb) / Dx, (y - yb) / Dy (:53-54)
+    double re, im;  // the value with the centre phase removed and the constant factor (:48-51)
+    int i0, j0;     // first footprint column and row, unwrapped (floor(M/2 + t) - ms)
+};
+
+// The pre-compensation factors exp(b D^2 ds^2) of every grid offset ds a
+// footprint can reach (FP64, stored as FP32 for the FP32 spread):
+// tab[ds + off], ds in [-off, n - off).
+__global__ void k_t3_table(float *__restrict__ tab, int n, int off, double bD2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = static_cast<double>(i - off);
+    tab[i] = static_cast<float>(exp(bD2 * d * d));
+}
+
+// Per point: the record fields and its tile; the rank within the tile from
+// the tile's counter.
+template <typename C2>
+__global__ void k_t3_prep(const double *__restrict__ x, const double *__restrict__ y, const C2 *__restrict__ f,
+                          long long n, Params P, int tiles_x, T3Rec *__restrict__ tmp, int2 *__restrict__ tile_rank,
+                          unsigned *__restrict__ counts) {
+    const long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (p >= n) return;
     const double xs = x[p] / P.kx, ys = y[p] / P.ky;  // :245-246
-    // value with the centre phase removed (:48-51) and the constant factor
     const double arg = P.sb * xs + P.tb * ys;
     double sa, ca;
     sincos(arg, &sa, &ca);
     const double fr = static_cast<double>(f[p].x), fi = static_cast<double>(f[p].y);
-    const double re = (fr * ca + fi * sa) * P.fact, im = (fi * ca - fr * sa) * P.fact;
-    const double x_temp = (xs - P.xb) / P.Dx, y_temp = (ys - P.yb) / P.Dy;  // :53-54
-    const long long nn_off = static_cast<long long>(floor(P.Mrx / 2 + x_temp));
-    const long long mm_off = static_cast<long long>(floor(P.Mry / 2 + y_temp));
-    const int W = 2 * P.ms + 1;
-    for (int c = lane; c < W; c += 32) {
-        const long long i = c - P.ms + nn_off;
-        const double dsi = static_cast<double>(i - P.Mrx / 2);
-        const double ex = P.b * P.Dx * P.Dx * dsi * dsi - P.t1 * (x_temp - dsi) * (x_temp - dsi);
-        const int ii = wrap(i, P.Mrx);
-        for (int r = 0; r < W; ++r) {
-            const long long j = r - P.ms + mm_off;
-            const double dsj = static_cast<double>(j - P.Mry / 2);
-            const double e = exp(ex + P.b * P.Dy * P.Dy * dsj * dsj - P.t1 * (y_temp - dsj) * (y_temp - dsj));  // :74
-            Real *cell = reinterpret_cast<Real *>(grid + static_cast<size_t>(wrap(j, P.Mry)) * P.Mrx + ii);
-            atomicAdd(cell, static_cast<Real>(re * e));
-            atomicAdd(cell + 1, static_cast<Real>(im * e));
+    T3Rec r;
+    r.re = (fr * ca + fi * sa) * P.fact;
+    r.im = (fi * ca - fr * sa) * P.fact;
+    r.xt = (xs - P.xb) / P.Dx;
+    r.yt = (ys - P.yb) / P.Dy;
+    r.i0 = static_cast<int>(floor(P.Mrx / 2 + r.xt)) - P.ms;
+    r.j0 = static_cast<int>(floor(P.Mry / 2 + r.yt)) - P.ms;
+    const int tile = (wrap(r.j0, P.Mry) / kT3Tile) * tiles_x + wrap(r.i0, P.Mrx) / kT3Tile;
+    tmp[p] = r;
+    tile_rank[p] = make_int2(tile, static_cast<int>(atomicAdd(counts + tile, 1u)));
+}
+
+// One CTA: exclusive scan of the tile counts into starts, and of the work
+// items per tile; counts[ntiles] receives the number of work items.
+__global__ void __launch_bounds__(1024) k_t3_scan(unsigned *__restrict__ counts, int ntiles,
+                                                  unsigned *__restrict__ starts, unsigned *__restrict__ item_starts) {
+    __shared__ unsigned s_pts[32], s_items[32];
+    __shared__ unsigned carry_pts, carry_items;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry_pts = carry_items = 0;
+    __syncthreads();
+    for (int base = 0; base < ntiles; base += 1024) {
+        const int i = base + tid;
+        const unsigned c = i < ntiles ? counts[i] : 0u;
+        const unsigned it = (c + kT3Item - 1) / kT3Item;
+        unsigned a = c, b = it;  // inclusive warp scans
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+            if (lane >= o) {
+                a += ua;
+                b += ub;
+            }
         }
+        if (lane == 31) {
+            s_pts[warp] = a;
+            s_items[warp] = b;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned wa = s_pts[lane], wb = s_items[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned ua = __shfl_up_sync(0xffffffffu, wa, o), ub = __shfl_up_sync(0xffffffffu, wb, o);
+                if (lane >= o) {
+                    wa += ua;
+                    wb += ub;
+                }
+            }
+            s_pts[lane] = wa;
+            s_items[lane] = wb;
+        }
+        __syncthreads();
+        const unsigned before_pts = carry_pts + (warp ? s_pts[warp - 1] : 0u) + a - c;
+        const unsigned before_items = carry_items + (warp ? s_items[warp - 1] : 0u) + b - it;
+        if (i < ntiles) {
+            starts[i] = before_pts;
+            item_starts[i] = before_items;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            carry_pts += s_pts[31];
+            carry_items += s_items[31];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) counts[ntiles] = carry_items;
+}
+
+// Records to their tile's range; the tile's work items {tile, first, count}.
+__global__ void k_t3_scatter(const T3Rec *__restrict__ tmp, const int2 *__restrict__ tile_rank, long long n,
+                             const unsigned *__restrict__ starts, T3Rec *__restrict__ recs) {
+    const long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (p >= n) return;
+    const int2 tr = tile_rank[p];
+    recs[starts[tr.x] + static_cast<unsigned>(tr.y)] = tmp[p];
+}
+
+__global__ void k_t3_items(const unsigned *__restrict__ counts, const unsigned *__restrict__ starts,
+                           const unsigned *__restrict__ item_starts, int ntiles, int4 *__restrict__ items) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    const unsigned c = counts[t];
+    for (unsigned k = 0; k * kT3Item < c; ++k)
+        items[item_starts[t] + k] = make_int4(t, static_cast<int>(starts[t] + k * kT3Item),
+                                              static_cast<int>(min(static_cast<unsigned>(kT3Item), c - k * kT3Item)),
+                                              0);
+}
+
+// Dynamic shared memory of a spreading CTA: the patch, then B points'
+// row and column weights, values, patch origins and fractional offsets.
+__host__ __device__ inline size_t t3_spread_smem(int W, int B, size_t real_bytes) {
+    const size_t PP = static_cast<size_t>(kT3Tile + W - 1);
+    return PP * PP * 2 * real_bytes + static_cast<size_t>(B) * (2 * W + 2) * real_bytes +
+           static_cast<size_t>(B) * (sizeof(int2) + sizeof(float2)) + 16;
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kT3Warps * 32)
+    k_t3_spread(const T3Rec *__restrict__ recs, const int4 *__restrict__ items, const unsigned *__restrict__ n_items,
+                Params P, int tiles_x, int B, const float *__restrict__ prex, int tabo_x, const float *__restrict__ prey,
+                int tabo_y, Real *__restrict__ grid) {
+    extern __shared__ __align__(16) unsigned char t3_smem[];
+    const int it = blockIdx.x;
+    if (it >= static_cast<int>(*n_items)) return;
+    const int4 item = items[it];
+    const int W = 2 * P.ms + 1, PP = kT3Tile + W - 1;
+    Real *patch = reinterpret_cast<Real *>(t3_smem);  // PP x PP complex, row-major
+    Real *wgt = patch + 2 * PP * PP;                  // per point: W row weights, then W column weights
+    Real *pval = wgt + 2 * B * W;                     // per point: the value
+    int2 *pinfo = reinterpret_cast<int2 *>(pval + 2 * B);  // per point: patch row, column of its first cell
+    float2 *pfrac = reinterpret_cast<float2 *>(pinfo + B);  // per point: fractional x, y offsets
+    const float t1f = static_cast<float>(P.t1);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < 2 * PP * PP; i += blockDim.x) patch[i] = Real(0);
+    const int tr0 = (item.x / tiles_x) * kT3Tile, tc0 = (item.x % tiles_x) * kT3Tile;  // tile origin (wrapped)
+    for (int b0 = 0; b0 < item.z; b0 += B) {
+        const int nb = min(B, item.z - b0);
+        __syncthreads();  // the previous batch's weights are consumed (and the patch zeroed)
+        // per point: its patch origin and value; weights: point q, k < W rows
+        // then W columns (:61-74), FP64 exponentials
+        for (int q = tid; q < nb; q += blockDim.x) {
+            const T3Rec &r = recs[item.y + b0 + q];
+            pinfo[q] = make_int2(wrap(r.j0, P.Mry) - tr0, wrap(r.i0, P.Mrx) - tc0);
+            pval[2 * q] = static_cast<Real>(r.re);
+            pval[2 * q + 1] = static_cast<Real>(r.im);
+            // fractional offsets within the first cell: the Gaussian's argument
+            // yt - dsj = fy + ms - k (exact integer part, FP64 difference once)
+            pfrac[q] = make_float2(static_cast<float>(r.xt - floor(r.xt)), static_cast<float>(r.yt - floor(r.yt)));
+        }
+        __syncthreads();
+        for (int e = tid; e < nb * 2 * W; e += blockDim.x) {
+            const int q = e / (2 * W), k = e - q * 2 * W;
+            const T3Rec &r = recs[item.y + b0 + q];
+            const bool row = k < W;
+            const int kk = row ? k : k - W;
+            const int ds = row ? r.j0 + kk - P.Mry / 2 : r.i0 + kk - P.Mrx / 2;  // dsj or dsi (:61-74)
+            if constexpr (sizeof(Real) == sizeof(double)) {
+                const double d = static_cast<double>(ds);
+                const double t = row ? r.yt : r.xt;
+                const double D = row ? P.Dy : P.Dx;
+                wgt[q * 2 * W + k] = exp(P.b * D * D * d * d - P.t1 * (t - d) * (t - d));
+            } else {
+                // FP32 data: exp(b D^2 ds^2) from the table (FP64-computed),
+                // the Gaussian exp(-t1 (frac + ms - k)^2) in FP32 on an exact
+                // argument
+                const float fr = row ? pfrac[q].y : pfrac[q].x;
+                const float g = fr + static_cast<float>(P.ms - kk);
+                const int ti = row ? min(max(ds + tabo_y, 0), 2 * tabo_y)
+                                   : min(max(ds + tabo_x, 0), 2 * tabo_x);  // inside the table by construction
+                const float pre = row ? prey[ti] : prex[ti];
+                wgt[q * 2 * W + k] = pre * expf(-t1f * g * g);
+            }
+        }
+        __syncthreads();
+        for (int q = 0; q < nb; ++q) {
+            // footprint origin in the patch: the tile offset of the first cell
+            const int2 o = pinfo[q];
+            const int lr = o.x, lc = o.y;
+            const Real *wr = wgt + q * 2 * W, *wc = wr + W;
+            const Real vr = pval[2 * q], vi = pval[2 * q + 1];
+            // this lane's columns c = lane + 32 m of the footprint: v * wc(c)
+            for (int c0 = 0; c0 < W; c0 += 32) {
+                const int c = c0 + lane;
+                if (c >= W) continue;
+                const Real ax = vr * wc[c], ay = vi * wc[c];
+                Real *col = patch + 2 * (lc + c);
+#pragma unroll 4
+                for (int k = (warp - lr % kT3Warps + kT3Warps) % kT3Warps; k < W; k += kT3Warps) {
+                    Real *cell = col + 2 * (lr + k) * PP;  // patch row lr + k = warp (mod 8)
+                    const Real w = wr[k];
+                    cell[0] += ax * w;
+                    cell[1] += ay * w;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < PP * PP; i += blockDim.x) {
+        const Real ax = patch[2 * i], ay = patch[2 * i + 1];
+        if (ax == Real(0) && ay == Real(0)) continue;
+        const int pr = i / PP, pc = i - pr * PP;
+        Real *g = grid + 2 * (static_cast<size_t>(wrap(tr0 + pr, P.Mry)) * P.Mrx + wrap(tc0 + pc, P.Mrx));
+        atomicAdd(g, ax);
+        atomicAdd(g + 1, ay);
     }
 }
 
-template <typename C2>
+// ---------------------------------------------------------------------------
+// Gathering (:156-194).  The Gaussian weight of tap (r, c) is
+// exp(-t1 (difs - npj)^2) exp(-t1 (dift - npi)^2) and the shift's (-1)^(i+j)
+// (:147-148) is (-1)^i (-1)^j, so both factor per column and per row.  A
+// warp owns 32 output frequencies: each lane sets up one of them (FP64:
+// scaling, cell, fractional offsets, the post-compensation and the centres'
+// phase), then the warp sums the footprints one frequency after the other --
+// lane l owns footprint columns l and l + 32 and runs down the rows -- and
+// the lane that owns the frequency finishes it.  FP32 data take the
+// Gaussian factors in FP32 on exact arguments (fractional offset + integer).
+// ---------------------------------------------------------------------------
+template <typename C2, typename Real>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_t3_gather(const double *__restrict__ s, const double *__restrict__ t, long long n, Params P,
                 const C2 *__restrict__ grid, C2 *__restrict__ F) {
-    const long long k = blockIdx.x * static_cast<long long>(kWarpsPerBlock) + (threadIdx.x >> 5);
+    const long long k0 = (blockIdx.x * static_cast<long long>(kWarpsPerBlock) + (threadIdx.x >> 5)) * 32;
     const int lane = threadIdx.x & 31;
-    if (k >= n) return;
-    const double ss = s[k] * P.kx, ts = t[k] * P.ky;  // :247-248
-    const double us = P.Mrx / 2 + (ss - P.sb), ut = P.Mry / 2 + (ts - P.tb);  // Ds = Dt = 1 (:163-166)
-    const long long nsn = static_cast<long long>(floor(us)), ntn = static_cast<long long>(floor(ut));
-    const double difs = us - nsn, dift = ut - ntn;
+    if (k0 >= n) return;
+    const long long k = k0 + lane;
+    const bool mine = k < n;
+    // this lane's frequency (:163-172, :189)
+    double ss = 0.0, ts = 0.0;
+    if (mine) {
+        ss = s[k] * P.kx;  // :247-248
+        ts = t[k] * P.ky;
+    }
+    const double us = P.Mrx / 2 + (ss - P.sb), ut = P.Mry / 2 + (ts - P.tb);  // Ds = Dt = 1
+    const double fs = floor(us), ft = floor(ut);
+    const Real difs = static_cast<Real>(us - fs), dift = static_cast<Real>(ut - ft);
+    const int ifirst = wrap(static_cast<long long>(fs) - P.ms + P.Mrx / 2, P.Mrx);
+    const int jfirst = wrap(static_cast<long long>(ft) - P.ms + P.Mry / 2, P.Mry);
     const int W = 2 * P.ms + 1;
-    double a0 = 0.0, a1 = 0.0;
-    for (int c = lane; c < W; c += 32) {
-        const long long nn = nsn - P.ms + c;  // shifted column; source column (nn + Mrx/2) mod Mrx
-        const double npj = static_cast<double>(c - P.ms);
-        const double es = -P.t1 * (difs - npj) * (difs - npj);
-        const int i = wrap(nn + P.Mrx / 2, P.Mrx);
-        for (int r = 0; r < W; ++r) {
-            const long long mm = ntn - P.ms + r;
-            const double npi = static_cast<double>(r - P.ms);
-            const double e = exp(es - P.t1 * (dift - npi) * (dift - npi));  // :182
-            const int j = wrap(mm + P.Mry / 2, P.Mry);
-            const C2 v = grid[static_cast<size_t>(j) * P.Mrx + i];
-            const double sg = ((i + j) & 1) ? -e : e;  // the (-1)^(i+j) of :147-148
-            a0 += static_cast<double>(v.x) * sg;
-            a1 += static_cast<double>(v.y) * sg;
+    const Real t1 = static_cast<Real>(P.t1);
+    Real res0 = Real(0), res1 = Real(0);
+    const int nk = static_cast<int>(min(32LL, n - k0));
+    for (int o = 0; o < nk; ++o) {
+        const Real ds = __shfl_sync(0xffffffffu, difs, o), dt = __shfl_sync(0xffffffffu, dift, o);
+        const int i0 = __shfl_sync(0xffffffffu, ifirst, o), j0 = __shfl_sync(0xffffffffu, jfirst, o);
+        // row weights of rows lane + 32 m (the grid has even sides: the
+        // wrapped row's parity is that of j0 + r)
+        Real wrow[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const int r = lane + 32 * m;
+            const Real g = dt - static_cast<Real>(r - P.ms);
+            const Real e = r < W ? exp(-t1 * g * g) : Real(0);
+            wrow[m] = ((j0 + r) & 1) ? -e : e;
+        }
+        Real acc0 = Real(0), acc1 = Real(0);
+        for (int c0 = 0; c0 < W; c0 += 32) {
+            const int c = c0 + lane;
+            const bool on = c < W;
+            const int cc = on ? c : 0;
+            const int i = i0 + cc >= P.Mrx ? i0 + cc - P.Mrx : i0 + cc;
+            const Real g = ds - static_cast<Real>(cc - P.ms);
+            const Real es = exp(-t1 * g * g);
+            // lanes past the footprint read a valid cell and weigh it by 0
+            const Real wcol = on ? (((i0 + cc) & 1) ? -es : es) : Real(0);
+            const C2 *col = grid + i;
+            Real s0 = Real(0), s1 = Real(0);
+            int j = j0;
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {  // footprint rows 32 m .. 32 m + 31
+                const int rn = min(32, W - 32 * m);
+#pragma unroll 8
+                for (int rr = 0; rr < rn; ++rr) {
+                    const Real wr = __shfl_sync(0xffffffffu, wrow[m], rr);
+                    const C2 v = col[static_cast<size_t>(j) * P.Mrx];
+                    s0 += static_cast<Real>(v.x) * wr;
+                    s1 += static_cast<Real>(v.y) * wr;
+                    j = j + 1 == P.Mry ? 0 : j + 1;
+                }
+            }
+            acc0 += s0 * wcol;
+            acc1 += s1 * wcol;
+        }
+        for (int x = 16; x > 0; x >>= 1) {
+            acc0 += __shfl_xor_sync(0xffffffffu, acc0, x);
+            acc1 += __shfl_xor_sync(0xffffffffu, acc1, x);
+        }
+        if (lane == o) {
+            res0 = acc0;
+            res1 = acc1;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-    }
-    if (lane == 0) {
+    if (mine) {
         double tmp1 = P.Dy * (ts - P.tb);
         tmp1 = tmp1 * tmp1;
         double tmp2 = P.Dx * (ss - P.sb);
@@ -157,10 +410,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const double arg = (ss - P.sb) * P.xb + (ts - P.tb) * P.yb;   // :189
         double sa, ca;
         sincos(arg, &sa, &ca);
-        C2 o;
-        o.x = static_cast<decltype(o.x)>((a0 * ca + a1 * sa) * comp);
-        o.y = static_cast<decltype(o.x)>((a1 * ca - a0 * sa) * comp);
-        F[k] = o;
+        const double a0 = static_cast<double>(res0), a1 = static_cast<double>(res1);
+        C2 out;
+        out.x = static_cast<decltype(out.x)>((a0 * ca + a1 * sa) * comp);
+        out.y = static_cast<decltype(out.x)>((a1 * ca - a0 * sa) * comp);
+        F[k] = out;
     }
 }
 
@@ -194,7 +448,10 @@ struct Scratch {
     cufftHandle plan = 0;
     bool plan_ok = false;
     ~Scratch() {
-        if (plan_ok) cufftDestroy(plan);
+        if (plan_ok) {
+            cudaStreamSynchronize(st);  // no FFT in flight when the handle goes back to the pool
+            nfft2d::pooled_plan_release(plan);
+        }
         if (grid) cudaFreeAsync(grid, st);
         if (mm) cudaFreeAsync(mm, st);
     }
@@ -262,21 +519,77 @@ extern "C" int nfft2d_nufft3_2d(const double *x, const double *y, const double *
     P.fact = f0 * f0;
 
     const bool dbl = precision == NFFT2D_F64;
+    const int W = 2 * P.ms + 1;
+    if (W > 96) return NFFT2D_ERR_UNSUPPORTED;  // the gather's lanes hold at most 96 row weights
+    const size_t rb = dbl ? sizeof(double) : sizeof(float);
+    int B = 32;  // points per weight batch of the spread
+    while (B > 4 && t3_spread_smem(W, B, rb) > 227 * 1024) B /= 2;
+    const size_t smem = t3_spread_smem(W, B, rb);
+    if (smem > 227 * 1024) return NFFT2D_ERR_UNSUPPORTED;
     const size_t cells = static_cast<size_t>(P.Mrx) * P.Mry;
-    const size_t csz = dbl ? sizeof(double2) : sizeof(float2);
-    T3_CUDA(cudaMallocAsync(&S.grid, cells * csz, st));
+    const size_t csz = 2 * rb;
+    const int tiles_x = (P.Mrx + kT3Tile - 1) / kT3Tile, tiles_y = (P.Mry + kT3Tile - 1) / kT3Tile;
+    const long long ntiles = static_cast<long long>(tiles_x) * tiles_y;
+    const long long max_items = ntiles + len_in / kT3Item + 1;
+    if (len_in > 0x7fffffffLL || max_items > 0x7fffffffLL) return NFFT2D_ERR_UNSUPPORTED;
+    // work buffers: grid, records (unsorted, sorted), tile/rank, counts, starts, item starts, items
+    const size_t off_tmp = (cells * csz + 255) / 256 * 256;
+    const size_t off_recs = off_tmp + (static_cast<size_t>(len_in) * sizeof(T3Rec) + 255) / 256 * 256;
+    const size_t off_tr = off_recs + (static_cast<size_t>(len_in) * sizeof(T3Rec) + 255) / 256 * 256;
+    const size_t off_cnt = off_tr + (static_cast<size_t>(len_in) * sizeof(int2) + 255) / 256 * 256;
+    const size_t off_st = off_cnt + (static_cast<size_t>(ntiles + 1) * sizeof(unsigned) + 255) / 256 * 256;
+    const size_t off_ist = off_st + (static_cast<size_t>(ntiles) * sizeof(unsigned) + 255) / 256 * 256;
+    const size_t off_items = off_ist + (static_cast<size_t>(ntiles) * sizeof(unsigned) + 255) / 256 * 256;
+    // pre-compensation tables over ds in [-off, off]: |ds| <= M/4 + ms + 1 for
+    // points inside the extents, off = M/2 + ms + 2 leaves margin
+    const int tabo_x = P.Mrx / 2 + P.ms + 2, tabo_y = P.Mry / 2 + P.ms + 2;
+    const size_t off_tx = off_items + (static_cast<size_t>(max_items) * sizeof(int4) + 255) / 256 * 256;
+    const size_t off_ty = off_tx + (static_cast<size_t>(2 * tabo_x + 1) * sizeof(float) + 255) / 256 * 256;
+    const size_t total = off_ty + static_cast<size_t>(2 * tabo_y + 1) * sizeof(float);
+    T3_CUDA(cudaMallocAsync(&S.grid, total, st));
+    unsigned char *base = static_cast<unsigned char *>(S.grid);
+    T3Rec *tmp = reinterpret_cast<T3Rec *>(base + off_tmp), *recs = reinterpret_cast<T3Rec *>(base + off_recs);
+    int2 *tr = reinterpret_cast<int2 *>(base + off_tr);
+    unsigned *counts = reinterpret_cast<unsigned *>(base + off_cnt), *starts = reinterpret_cast<unsigned *>(base + off_st);
+    unsigned *istarts = reinterpret_cast<unsigned *>(base + off_ist);
+    int4 *items = reinterpret_cast<int4 *>(base + off_items);
+    float *prex = reinterpret_cast<float *>(base + off_tx), *prey = reinterpret_cast<float *>(base + off_ty);
+    k_t3_table<<<(2 * tabo_x + 1 + 255) / 256, 256, 0, st>>>(prex, 2 * tabo_x + 1, tabo_x, P.b * P.Dx * P.Dx);
+    k_t3_table<<<(2 * tabo_y + 1 + 255) / 256, 256, 0, st>>>(prey, 2 * tabo_y + 1, tabo_y, P.b * P.Dy * P.Dy);
+    T3_CUDA(cudaGetLastError());
     T3_CUDA(cudaMemsetAsync(S.grid, 0, cells * csz, st));
-    const unsigned blk_in = static_cast<unsigned>((len_in + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    const unsigned blk_out = static_cast<unsigned>((len_out + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    T3_CUDA(cudaMemsetAsync(counts, 0, static_cast<size_t>(ntiles + 1) * sizeof(unsigned), st));
+    const unsigned pb = static_cast<unsigned>((len_in + 255) / 256);
     if (dbl)
-        k_t3_spread<double2, double><<<blk_in, kWarpsPerBlock * 32, 0, st>>>(
-            x, y, static_cast<const double2 *>(f), len_in, P, static_cast<double2 *>(S.grid));
+        k_t3_prep<double2><<<pb, 256, 0, st>>>(x, y, static_cast<const double2 *>(f), len_in, P, tiles_x, tmp, tr,
+                                              counts);
     else
-        k_t3_spread<float2, float><<<blk_in, kWarpsPerBlock * 32, 0, st>>>(
-            x, y, static_cast<const float2 *>(f), len_in, P, static_cast<float2 *>(S.grid));
+        k_t3_prep<float2><<<pb, 256, 0, st>>>(x, y, static_cast<const float2 *>(f), len_in, P, tiles_x, tmp, tr,
+                                             counts);
+    T3_CUDA(cudaGetLastError());
+    k_t3_scan<<<1, 1024, 0, st>>>(counts, static_cast<int>(ntiles), starts, istarts);
+    T3_CUDA(cudaGetLastError());
+    k_t3_scatter<<<pb, 256, 0, st>>>(tmp, tr, len_in, starts, recs);
+    T3_CUDA(cudaGetLastError());
+    k_t3_items<<<static_cast<unsigned>((ntiles + 255) / 256), 256, 0, st>>>(counts, starts, istarts,
+                                                                           static_cast<int>(ntiles), items);
+    T3_CUDA(cudaGetLastError());
+    // one CTA per possible work item; those beyond the device-side count return
+    if (dbl) {
+        T3_CUDA(cudaFuncSetAttribute(k_t3_spread<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+        k_t3_spread<double><<<static_cast<unsigned>(max_items), kT3Warps * 32, smem, st>>>(
+            recs, items, counts + ntiles, P, tiles_x, B, prex, tabo_x, prey, tabo_y, static_cast<double *>(S.grid));
+    } else {
+        T3_CUDA(cudaFuncSetAttribute(k_t3_spread<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+        k_t3_spread<float><<<static_cast<unsigned>(max_items), kT3Warps * 32, smem, st>>>(
+            recs, items, counts + ntiles, P, tiles_x, B, prex, tabo_x, prey, tabo_y, static_cast<float *>(S.grid));
+    }
     T3_CUDA(cudaGetLastError());
     // :283-292 -- rows are Mry, the fast (column) dimension Mrx
-    if (cufftPlan2d(&S.plan, P.Mry, P.Mrx, dbl ? CUFFT_Z2Z : CUFFT_C2C) != CUFFT_SUCCESS) return NFFT2D_ERR_CUFFT;
+    if (nfft2d::pooled_plan_2d(&S.plan, P.Mry, P.Mrx, dbl ? CUFFT_Z2Z : CUFFT_C2C) != CUFFT_SUCCESS)
+        return NFFT2D_ERR_CUFFT;
     S.plan_ok = true;
     if (cufftSetStream(S.plan, st) != CUFFT_SUCCESS) return NFFT2D_ERR_CUFFT;
     const cufftResult fr =
@@ -285,14 +598,14 @@ extern "C" int nfft2d_nufft3_2d(const double *x, const double *y, const double *
             : cufftExecC2C(S.plan, static_cast<cufftComplex *>(S.grid), static_cast<cufftComplex *>(S.grid),
                            CUFFT_FORWARD);
     if (fr != CUFFT_SUCCESS) return NFFT2D_ERR_CUFFT;
+    const long long warps_out = (len_out + 31) / 32;  // 32 frequencies per warp
+    const unsigned blk_out = static_cast<unsigned>((warps_out + kWarpsPerBlock - 1) / kWarpsPerBlock);
     if (dbl)
-        k_t3_gather<double2><<<blk_out, kWarpsPerBlock * 32, 0, st>>>(s, t, len_out, P,
-                                                                     static_cast<const double2 *>(S.grid),
-                                                                     static_cast<double2 *>(F));
+        k_t3_gather<double2, double><<<blk_out, kWarpsPerBlock * 32, 0, st>>>(
+            s, t, len_out, P, static_cast<const double2 *>(S.grid), static_cast<double2 *>(F));
     else
-        k_t3_gather<float2><<<blk_out, kWarpsPerBlock * 32, 0, st>>>(s, t, len_out, P,
-                                                                    static_cast<const float2 *>(S.grid),
-                                                                    static_cast<float2 *>(F));
+        k_t3_gather<float2, float><<<blk_out, kWarpsPerBlock * 32, 0, st>>>(
+            s, t, len_out, P, static_cast<const float2 *>(S.grid), static_cast<float2 *>(F));
     T3_CUDA(cudaGetLastError());
     return cuda_status(cudaStreamSynchronize(st));
 }

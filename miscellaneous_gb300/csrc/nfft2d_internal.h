@@ -137,6 +137,7 @@ struct nfft2d_plan_s {
     long long n_chunks = 0;
     double xscale1 = 1.0, xscale2 = 1.0;  // dt/dx for the units given to set_points
 
+    bool strips = true;  // strip-major cell order (false: row-major, a gather-only plan)
     cufftHandle fft = 0;
     bool fft_ok = false;
     cufftHandle fft_rows = 0, fft_cols = 0;  // pruned 1D passes (see run_fft)
@@ -171,7 +172,11 @@ int gather_smem_bytes(const nfft2d_plan_s *p);
 cudaError_t launch_spread(const nfft2d_plan_s *p, const void *f);
 
 // Geometry for given parameters; returns NFFT2D_OK or an error status.
-int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1, int *n2);
+// strips = false bins a tile's cells row by row (strip width = tile): for
+// plans that only gather, whose warps then read fewer distinct rows; their
+// spreads take the direct kernel.
+int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1, int *n2,
+                   bool strips = true);
 
 int grid_blocks(const nfft2d_plan_s *p, const void *kernel, int threads, int smem);
 
@@ -180,7 +185,7 @@ int grid_blocks(const nfft2d_plan_s *p, const void *kernel, int threads, int sme
 // creates no cuFFT plan of its own (the batch runs the FFTs); tile = 0 picks
 // the default tile.
 int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int precision, int tile,
-                cudaStream_t stream, void *ext_grid);
+                cudaStream_t stream, void *ext_grid, bool strips = true);
 void release_plan(nfft2d_plan_s *p);
 int tensor_map_for(nfft2d_plan_s *p);
 

@@ -553,7 +553,8 @@ int nfft2d_knab_set_points(nfft2d_knab k, int len1, int len2, const void *rho_ou
             release_plan(k->plan);
             k->plan = nullptr;
         }
-        if ((st = create_plan(&k->plan, N1, N2, kSigma, kKernelK, k->precision, 0, k->stream, nullptr)) !=
+        // the regridder only gathers: row-major cell order (fewer distinct rows per warp)
+        if ((st = create_plan(&k->plan, N1, N2, kSigma, kKernelK, k->precision, 0, k->stream, nullptr, false)) !=
             NFFT2D_OK)
             return st;
     }

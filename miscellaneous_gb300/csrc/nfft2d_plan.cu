@@ -1062,7 +1062,8 @@ dim3 row_grid(int cols, int rows) {
 // ===========================================================================
 namespace nfft2d {
 
-int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1o, int *n2o) {
+int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile, Geom *g, int *n1o, int *n2o,
+                   bool strips) {
     if (N1 <= 0 || N2 <= 0 || (N1 & 1) || (N2 & 1)) return NFFT2D_ERR_INVALID_ARG;
     if (K < kMinK || K > kMaxK) return NFFT2D_ERR_INVALID_ARG;
     if (precision != NFFT2D_F32 && precision != NFFT2D_F64) return NFFT2D_ERR_INVALID_ARG;
@@ -1092,7 +1093,7 @@ int compute_layout(int N1, int N2, double sigma, int K, int precision, int tile,
     g->Ke = K + (K & 1);
     // strip-major cell order inside a tile where the register spread runs
     // (FP32, 16 x 16 tiles), plain row-major elsewhere
-    g->SW = (precision == NFFT2D_F32 && T == 16) ? spread_strip_width(K) : T;
+    g->SW = (strips && precision == NFFT2D_F32 && T == 16) ? spread_strip_width(K) : T;
     g->PR = T + 2 * K;
     // Patch row pitch: the T + 2Ke columns a tile needs, rounded up to 16
     // complex (128 bytes); with it a warp's reads of one tap spread over the
@@ -1321,11 +1322,11 @@ int nfft2d_layout_query(int N1, int N2, double sigma, int K, int precision, int 
 namespace nfft2d {
 
 int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int precision, int tile,
-                cudaStream_t stream, void *ext_grid) {
+                cudaStream_t stream, void *ext_grid, bool strips) {
     if (!out) return NFFT2D_ERR_INVALID_ARG;
     *out = nullptr;
     Geom g{};
-    int st = compute_layout(N1, N2, sigma, K, precision, tile, &g, nullptr, nullptr);
+    int st = compute_layout(N1, N2, sigma, K, precision, tile, &g, nullptr, nullptr, strips);
     if (st != NFFT2D_OK) return st;
     nfft2d_plan_s *p = new (std::nothrow) nfft2d_plan_s();
     if (!p) return NFFT2D_ERR_OOM;
@@ -1335,6 +1336,7 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     p->sigma = sigma;
     p->precision = precision;
     p->g = g;
+    p->strips = strips;
     p->stream = stream;
     p->grid = ext_grid;
     p->grid_external = ext_grid != nullptr;
@@ -1429,7 +1431,7 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     if (!p || !t) return NFFT2D_ERR_INVALID_ARG;
     if (t->tile != 0 && t->tile != p->g.T) {
         Geom g{};
-        int st = compute_layout(p->N1, p->N2, p->sigma, p->K, p->precision, t->tile, &g, nullptr, nullptr);
+        int st = compute_layout(p->N1, p->N2, p->sigma, p->K, p->precision, t->tile, &g, nullptr, nullptr, p->strips);
         if (st != NFFT2D_OK) return st;
         cudaStreamSynchronize(p->stream);
         p->g = g;

@@ -913,11 +913,11 @@ def run_ours(args, wl):
         # upload and the pass overlap; "copy": they are copied first.
         cs = torch.cuda.Stream(device=dev)
         ev_sp, ev_in, ev_fwd, ev_out = (torch.cuda.Event() for _ in range(4))
-        direct = args.e2e_coords == "direct"
+        mode = {"direct": args.e2e_coords == "direct"}
 
         def e2e_step():
             dF.copy_(hF, non_blocking=True)
-            if direct:
+            if mode["direct"]:
                 plan.set_points(hx1, hx2, units="unit", sync=False)
             else:
                 dx1.copy_(hx1, non_blocking=True)
@@ -939,6 +939,29 @@ def run_ours(args, wl):
             hF_out.copy_(F_out, non_blocking=True)
             stream.wait_event(ev_out)
 
+        # "auto": which coordinate path this machine's host link favours, from a
+        # short untimed trial of each (the kernel-read path measured 3.88 ms
+        # per config-3 step on some boxes and 4.8 ms on others, the copy
+        # path 4.14 ms on all), like the kernel autotuner's trial
+        trial = None
+        if args.e2e_coords == "auto":
+            trial = {}
+            for m in ("direct", "copy"):
+                mode["direct"] = m == "direct"
+                for _ in range(2):
+                    e2e_step()
+                    plan.synchronize()
+                ts = []
+                for _ in range(3):
+                    flush.zero_()
+                    ev0.record(stream)
+                    e2e_step()
+                    ev1.record(stream)
+                    ev1.synchronize()
+                    ts.append(ev0.elapsed_time(ev1))
+                    plan.synchronize()
+                trial[m] = statistics.median(ts)
+            mode["direct"] = trial["direct"] <= trial["copy"]
         for _ in range(args.warmup):
             e2e_step()
             plan.synchronize()
@@ -973,9 +996,9 @@ def run_ours(args, wl):
         e2e = {"value": world * M / (te * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te,
                "coords_upload_ms": cu, "coords_upload_gbs": (hx1.numel() + hx2.numel()) * 4 / (cu * 1e-3) / 1e9,
-               "coords": args.e2e_coords,
+               "coords": "direct" if mode["direct"] else "copy", "coords_trial_ms": trial,
                "includes": "H2D of F, the coordinates (read by the binning pass over the link with coords "
-                           "'direct', copied first with 'copy') and f, set_points (binning sort, enqueued "
+                           "'direct', copied first with 'copy'; the faster of the two in an untimed trial) and f, set_points (binning sort, enqueued "
                            "without a host round trip), forward, adjoint, D2H of f_out and F_out; f goes up "
                            "during the binning's tail and the forward, f_out comes down during the adjoint "
                            "(second stream); the plan status is read and L2 is flushed (256 MB written) after "
@@ -1748,9 +1771,9 @@ def main():
                          "cuFFT passes, fused")
     ap.add_argument("--io-order", choices=["caller", "binned"], default="caller",
                     help="per-point arrays of the timed steps in the caller's or the plan's binned order")
-    ap.add_argument("--e2e-coords", choices=["direct", "copy"], default="direct",
+    ap.add_argument("--e2e-coords", choices=["auto", "direct", "copy"], default="auto",
                     help="e2e: the binning reads the page-locked coordinates over the link (direct) or after "
-                         "a copy (copy)")
+                         "a copy (copy); auto picks the faster by an untimed trial of each")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
     ap.add_argument("--K", type=int, default=None,

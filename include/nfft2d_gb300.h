@@ -372,7 +372,9 @@ int nfft2d_knab_window(double T, double B, int P, int N, double *G, int G_len, i
 int nfft2d_knab_create(nfft2d_knab *knab, int Nrows, int Ncols, const double *rho_in, const double *cos_in,
                        double B1, double B2, int precision, void *stream);
 int nfft2d_knab_destroy(nfft2d_knab knab);
-/* Bind the output points (FP32 or FP64 coordinates); synchronizes. */
+/* Bind the output points (FP32 or FP64 coordinates): reads their extents
+ * back (synchronizes) and enqueues their binning on the regridder's stream,
+ * whose errors nfft2d_knab_synchronize reports. */
 int nfft2d_knab_set_points(nfft2d_knab knab, int len1, int len2, const void *rho_out, const void *cos_out,
                            int coord_dtype);
 /* Asynchronous on the stream given at creation. */

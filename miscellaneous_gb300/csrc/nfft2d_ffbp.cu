@@ -290,7 +290,9 @@ int leaf(Ffbp &F, int a, int b, const double *pho, const double *cs, long long n
             k_leaf_embed<float2><<<eb, 256, 0, F.st>>>(static_cast<const float2 *>(F.ph) + static_cast<size_t>(p) * F.nf,
                                                       F.nf, static_cast<float2 *>(F.leaf_F));
         FB_CUDA(cudaGetLastError());
-        FB_TRY(nfft2d_set_points(F.leaf, n, x1, x2, NFFT2D_COORD_F64, NFFT2D_UNITS_GRID));
+        // no host round trip per pulse: the transform reads the work-item
+        // count on the device; nfft2d_synchronize below reports errors
+        FB_TRY(nfft2d_set_points_async(F.leaf, n, x1, x2, NFFT2D_COORD_F64, NFFT2D_UNITS_GRID));
         FB_TRY(nfft2d_type2(F.leaf, -1, F.leaf_F, f));  // NFFT1_1D.m:43: fft, negative exponent
         if (F.prec == NFFT2D_F64)
             k_leaf_acc<double2><<<nb, 256, 0, F.st>>>(static_cast<const double2 *>(f), dr, n, k4fc, F.sar.c,

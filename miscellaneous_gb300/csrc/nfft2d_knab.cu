@@ -562,7 +562,9 @@ int nfft2d_knab_set_points(nfft2d_knab k, int len1, int len2, const void *rho_ou
     k->b = b;
     if ((st = upload_weights(k)) != NFFT2D_OK) return st;
     // grid-unit coordinates x1 = (c - cos_in[0]) b / T2, x2 = (r - rho_in[0]) a / T1 (Interp_2D.m:28)
-    st = set_points_scaled(k->plan, M, cos_out, rho_out, coord_dtype, b / k->T2, a / k->T1, k->cos0, k->rho0);
+    // the binning is enqueued (the extents above were the host round trip);
+    // nfft2d_knab_synchronize reports its errors
+    st = set_points_scaled(k->plan, M, cos_out, rho_out, coord_dtype, b / k->T2, a / k->T1, k->cos0, k->rho0, true);
     if (st != NFFT2D_OK) return st;
     k->points_valid = true;
     return NFFT2D_OK;

@@ -1110,6 +1110,7 @@ def run_ours(args, wl):
                                         "spreads its own M, NCCL sum all-reduce of the N1 x N2 adjoint" % world)
                            if world > 1 else "single GPU",
                            tuning=(tuned or {}).get("tuning"), plan=plan.info()),
+            "autotune_trials_ms": [{**c, "ms": round(ms, 4)} for c, ms in (tuned or {}).get("trials", [])] or None,
             "stages_ms": stage,
             "stages_note": STAGES_NOTE[fused],
             "forward_ms": stage["pad"] + stage["fft_fwd"] + stage["halo_fill"] + stage["gather"],

@@ -101,10 +101,11 @@ typedef struct {
 } nfft2d_info;
 
 typedef struct {
-    int tile;              /* 0 = default; else 8, 16, 32 or 64                 */
-    int chunk;             /* 0 = default; else points per work item (>= 32)    */
-    int gather_variant;    /* NFFT2D_VARIANT_*                                  */
-    int spread_variant;    /* NFFT2D_VARIANT_*                                  */
+    int tile;              /* 0 or -1 = keep; else 8, 16, 32 or 64              */
+    int chunk;             /* 0 or -1 = keep; else points per work item (>= 32) */
+    int gather_variant;    /* -1 = keep; NFFT2D_VARIANT_* (AUTO: chosen at
+                              set_points from the bin density)                  */
+    int spread_variant;    /* -1 = keep; NFFT2D_VARIANT_*                       */
     int compensated;       /* -1 = default (on); 0 off; 1 on (FP32 gather)      */
     int fft_mode;          /* -1 = keep.  Initially automatic: 2 below 2048 x
                               2048 oversampled cells where it applies, else 1

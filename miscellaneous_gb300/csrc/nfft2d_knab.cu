@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -122,7 +123,48 @@ double window_integral_theta(double t0, double t1, double B1, double TT, const G
 // f + [-B0/2, B0/2]) is [-B1/2, f + B0/2] for every f <= 0 with f + B0/2 <
 // B1/2 (because B0 >= B1), so G(k) is a cumulative integral of the window
 // from its left edge, accumulated panel by panel in theta.
+// Windows already computed in this process, by their exact parameters: an
+// FFBP image builds two windows per regridding (~0.1-0.3 ms each, 4000
+// Bessel evaluations), and every image of the same geometry asks for the
+// same ones.  Up to 1024 windows are kept, the oldest replaced first.
+struct WindowEntry {
+    double T, B;
+    int P;
+    long N;
+    long kg;
+    std::vector<double> G;
+};
+std::mutex g_win_mu;
+std::vector<WindowEntry> g_win_cache;
+size_t g_win_next = 0;
+
+long knab_window_compute(double T, double B, int P, long N, std::vector<double> *G);
+
 long knab_window(double T, double B, int P, long N, std::vector<double> *G) {
+    if (!G) return knab_window_compute(T, B, P, N, nullptr);
+    {
+        std::lock_guard<std::mutex> lock(g_win_mu);
+        for (const auto &e : g_win_cache)
+            if (e.T == T && e.B == B && e.P == P && e.N == N) {
+                *G = e.G;
+                return e.kg;
+            }
+    }
+    const long kg = knab_window_compute(T, B, P, N, G);
+    if (kg >= 0) {
+        std::lock_guard<std::mutex> lock(g_win_mu);
+        WindowEntry e{T, B, P, N, kg, *G};
+        if (g_win_cache.size() < 1024) {
+            g_win_cache.push_back(std::move(e));
+        } else {
+            g_win_cache[g_win_next] = std::move(e);
+            g_win_next = (g_win_next + 1) % g_win_cache.size();
+        }
+    }
+    return kg;
+}
+
+long knab_window_compute(double T, double B, int P, long N, std::vector<double> *G) {
     if (!(T > 0) || !(B > 0) || !(B < 1.0 / T) || N < 1 || P < 1 || !std::isfinite(T) || !std::isfinite(B))
         return -1;
     const double df = 1.0 / (static_cast<double>(N) * T);            // :16

@@ -1429,7 +1429,7 @@ int nfft2d_set_stream(nfft2d_plan p, void *stream) {
 
 int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
     if (!p || !t) return NFFT2D_ERR_INVALID_ARG;
-    if (t->tile != 0 && t->tile != p->g.T) {
+    if (t->tile > 0 && t->tile != p->g.T) {
         Geom g{};
         int st = compute_layout(p->N1, p->N2, p->sigma, p->K, p->precision, t->tile, &g, nullptr, nullptr, p->strips);
         if (st != NFFT2D_OK) return st;
@@ -1441,7 +1441,7 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
         if ((st = setup_grid(p)) != NFFT2D_OK) return st;
         if ((st = setup_bins(p)) != NFFT2D_OK) return st;
     }
-    if (t->chunk != 0) {
+    if (t->chunk != 0 && t->chunk != -1) {
         if (t->chunk < 32 || t->chunk > (1 << 20)) return NFFT2D_ERR_INVALID_ARG;
         if (t->chunk != p->chunk) {
             p->chunk = t->chunk;
@@ -1450,17 +1450,21 @@ int nfft2d_set_tuning(nfft2d_plan p, const nfft2d_tuning *t) {
         }
     }
     for (int v : {t->gather_variant, t->spread_variant})
-        if (v < NFFT2D_VARIANT_AUTO || v > NFFT2D_VARIANT_DIRECT) return NFFT2D_ERR_INVALID_ARG;
+        if (v < -1 || v > NFFT2D_VARIANT_DIRECT) return NFFT2D_ERR_INVALID_ARG;
     const int auto_v = p->precision == NFFT2D_F32 ? NFFT2D_VARIANT_TILED : NFFT2D_VARIANT_DIRECT;
-    const bool gauto = t->gather_variant == NFFT2D_VARIANT_AUTO && p->precision == NFFT2D_F32;
-    const int gv = gauto ? auto_gather(p, p->points_valid ? p->M : 0)
-                         : (t->gather_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->gather_variant);
-    const int sv = t->spread_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->spread_variant;
-    if (p->precision == NFFT2D_F64 && (gv == NFFT2D_VARIANT_TILED || sv == NFFT2D_VARIANT_TILED))
-        return NFFT2D_ERR_UNSUPPORTED;
-    p->gather_variant = gv;
-    p->gather_auto = gauto;
-    p->spread_variant = sv;
+    if (t->gather_variant >= 0) {  // -1 keeps the current choice (automatic or fixed)
+        const bool gauto = t->gather_variant == NFFT2D_VARIANT_AUTO && p->precision == NFFT2D_F32;
+        const int gv = gauto ? auto_gather(p, p->points_valid ? p->M : 0)
+                             : (t->gather_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->gather_variant);
+        if (p->precision == NFFT2D_F64 && gv == NFFT2D_VARIANT_TILED) return NFFT2D_ERR_UNSUPPORTED;
+        p->gather_variant = gv;
+        p->gather_auto = gauto;
+    }
+    if (t->spread_variant >= 0) {
+        const int sv = t->spread_variant == NFFT2D_VARIANT_AUTO ? auto_v : t->spread_variant;
+        if (p->precision == NFFT2D_F64 && sv == NFFT2D_VARIANT_TILED) return NFFT2D_ERR_UNSUPPORTED;
+        p->spread_variant = sv;
+    }
     if (t->compensated >= 0) p->compensated = t->compensated ? 1 : 0;
     if (t->io_order >= 0) {
         if (t->io_order != NFFT2D_ORDER_CALLER && t->io_order != NFFT2D_ORDER_BINNED) return NFFT2D_ERR_INVALID_ARG;

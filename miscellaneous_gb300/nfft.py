@@ -101,9 +101,11 @@ class Plan:
         self.stream = stream
         check(self._lib.nfft2d_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "nfft2d_set_stream")
 
-    def set_tuning(self, tile: int = 0, chunk: int = 0, gather_variant: int = 0, spread_variant: int = 0,
+    def set_tuning(self, tile: int = -1, chunk: int = -1, gather_variant: int = -1, spread_variant: int = -1,
                    compensated: int = -1, fft_mode: int = -1, io_order: str | None = None) -> None:
-        """fft_mode: -1 keep, 0 cuFFT 2D plan, 1 cuFFT row/band-column passes,
+        """Every argument left out keeps the plan's current setting.
+        gather_variant / spread_variant: _lib.VARIANT_AUTO, _TILED or _DIRECT.
+        fft_mode: -1 keep, 0 cuFFT 2D plan, 1 cuFFT row/band-column passes,
         2 hand-written passes fused with pad/fill/fold/crop (FP32, power-of-two
         grids; the default below 2048 x 2048 oversampled cells).
         io_order: None keep, 'caller' or 'binned' (per-point arrays in the

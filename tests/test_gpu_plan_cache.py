@@ -71,3 +71,21 @@ def test_fft_mode_change_takes_the_new_modes_plans():
     for mode in (0, 1):
         a, b = _run(N, M, seed=3, fft_mode=mode)
         assert _rel(a, a2) < 2e-6 and _rel(b, b2) < 2e-6, mode
+
+
+def test_tuning_arguments_left_out_keep_their_settings():
+    from miscellaneous_gb300 import _lib
+    from miscellaneous_gb300.nfft import Plan
+    x1, x2, F, f = _case(256, 100000, seed=5)
+    with Plan(256, 256) as p:
+        p.set_tuning(gather_variant=_lib.VARIANT_TILED, chunk=256)
+        p.set_points(x1, x2)
+        p.set_tuning(io_order="binned")
+        p.set_tuning(io_order="caller", fft_mode=0)
+        info = p.info()
+        assert info["gather_variant"] == _lib.VARIANT_TILED and info["chunk"] == 256 and info["fft_mode"] == 0
+        # back to the automatic choice: 100,000 points on 32 x 32 tiles of 16^2 cells is
+        # 98 points per tile, below the direct gather's 128
+        p.set_tuning(gather_variant=_lib.VARIANT_AUTO)
+        p.set_points(x1, x2)
+        assert p.info()["gather_variant"] == _lib.VARIANT_TILED

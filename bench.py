@@ -782,6 +782,7 @@ def run_ours(args, wl):
     from miscellaneous_gb300.shard import ShardedPlan
 
     world, rank, local = dist_env()
+    torch.cuda.set_device(local)  # before the process group: NCCL binds each rank to its device
     if world > 1:
         dist.init_process_group("nccl")
         # one transform of world * M points: each rank draws its own M points
@@ -790,7 +791,6 @@ def run_ours(args, wl):
             wl = clustered_config3(seed=3 + 1000 * rank, K=wl["K"])
         elif wl["name"].startswith("polar"):
             wl = polar_raster(seed=2 + 1000 * rank, K=wl["K"])
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     N1, N2, M = wl["N1"], wl["N2"], wl["x1"].size

@@ -167,7 +167,8 @@ static bool injected_alloc_failure() {
 // for the whole device, while callers that make and drop plans (the FFBP
 // recursion: two plans and a regridder per node) reuse the same sizes.  A
 // request takes the smallest cached block of at least its size and at most
-// twice it; freed blocks are kept up to 1 GiB, the oldest released first.
+// twice it, on the current device; freed blocks are kept up to 1 GiB, the
+// oldest released first.
 // Callers return a block only once no work of theirs that uses it is in
 // flight (they synchronize the stream first).
 namespace {
@@ -175,14 +176,14 @@ constexpr size_t kBlockCacheBytes = size_t(1) << 30;
 struct CachedBlock {
     void *p;
     size_t bytes;
+    int device;
     unsigned long long age;
 };
 std::mutex g_blk_mu;
-std::vector<CachedBlock> g_blk_free;
-std::vector<std::pair<void *, size_t>> g_blk_live;
+std::vector<CachedBlock> g_blk_free;  // released blocks
+std::vector<CachedBlock> g_blk_live;  // blocks handed out
 size_t g_blk_free_bytes = 0;
 unsigned long long g_blk_clock = 0;
-int g_blk_device = -1;
 }  // namespace
 
 cudaError_t nfft2d::plan_malloc(void **ptr, size_t bytes) {
@@ -194,32 +195,24 @@ cudaError_t nfft2d::plan_malloc(void **ptr, size_t bytes) {
     cudaGetDevice(&dev);
     {
         std::lock_guard<std::mutex> lock(g_blk_mu);
-        if (g_blk_device == dev) {
-            size_t best = g_blk_free.size();
-            for (size_t i = 0; i < g_blk_free.size(); ++i)
-                if (g_blk_free[i].bytes >= bytes && g_blk_free[i].bytes <= 2 * bytes + 4096 &&
-                    (best == g_blk_free.size() || g_blk_free[i].bytes < g_blk_free[best].bytes))
-                    best = i;
-            if (best < g_blk_free.size()) {
-                const CachedBlock b = g_blk_free[best];
-                g_blk_free.erase(g_blk_free.begin() + static_cast<long>(best));
-                g_blk_free_bytes -= b.bytes;
-                g_blk_live.push_back({b.p, b.bytes});
-                *ptr = b.p;
-                return cudaSuccess;
-            }
+        size_t best = g_blk_free.size();
+        for (size_t i = 0; i < g_blk_free.size(); ++i)
+            if (g_blk_free[i].device == dev && g_blk_free[i].bytes >= bytes && g_blk_free[i].bytes <= 2 * bytes + 4096 &&
+                (best == g_blk_free.size() || g_blk_free[i].bytes < g_blk_free[best].bytes))
+                best = i;
+        if (best < g_blk_free.size()) {
+            const CachedBlock b = g_blk_free[best];
+            g_blk_free.erase(g_blk_free.begin() + static_cast<long>(best));
+            g_blk_free_bytes -= b.bytes;
+            g_blk_live.push_back(b);
+            *ptr = b.p;
+            return cudaSuccess;
         }
     }
     const cudaError_t e = cudaMalloc(ptr, bytes);
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_blk_mu);
-    if (g_blk_device != dev) {  // blocks belong to one device: start over on another
-        for (const auto &b : g_blk_free) cudaFree(b.p);
-        g_blk_free.clear();
-        g_blk_free_bytes = 0;
-        g_blk_device = dev;
-    }
-    g_blk_live.push_back({*ptr, bytes});
+    g_blk_live.push_back({*ptr, bytes, dev, 0});
     return cudaSuccess;
 }
 
@@ -229,14 +222,15 @@ void nfft2d::plan_free(void *ptr) {
     {
         std::lock_guard<std::mutex> lock(g_blk_mu);
         size_t i = 0;
-        while (i < g_blk_live.size() && g_blk_live[i].first != ptr) ++i;
+        while (i < g_blk_live.size() && g_blk_live[i].p != ptr) ++i;
         if (i == g_blk_live.size()) {
             drop.push_back(ptr);  // not from plan_malloc
         } else {
-            const size_t bytes = g_blk_live[i].second;
+            CachedBlock b = g_blk_live[i];
             g_blk_live.erase(g_blk_live.begin() + static_cast<long>(i));
-            g_blk_free.push_back({ptr, bytes, ++g_blk_clock});
-            g_blk_free_bytes += bytes;
+            b.age = ++g_blk_clock;
+            g_blk_free.push_back(b);
+            g_blk_free_bytes += b.bytes;
             while (g_blk_free_bytes > kBlockCacheBytes && !g_blk_free.empty()) {
                 size_t old = 0;
                 for (size_t j = 1; j < g_blk_free.size(); ++j)

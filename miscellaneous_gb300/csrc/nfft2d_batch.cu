@@ -632,21 +632,35 @@ int nfft2d_batch_set_points(nfft2d_batch b, const long long *M, const void *cons
     b->points_valid = false;
     drop_graphs(b);
     B_TRY(cudaStreamSynchronize(b->stream));
-    // every transform's binning is enqueued on the batch stream without a
-    // host round trip, then the status words (work-item counts, errors) of
-    // all of them come back with one synchronisation
-    for (int i = 0; i < b->count; ++i) {  // internal order; the arguments are in the caller's
-        const int t = b->order[i];
-        const int st = nfft2d_set_points_async(b->plans[i], M[t], x1[t], x2[t], coord_dtype, units);
-        if (st != NFFT2D_OK) return st;
-    }
-    for (int i = 0; i < b->count; ++i)
-        B_TRY(cudaMemcpyAsync(b->plans[i]->h_status, b->plans[i]->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost,
-                              b->stream));
-    B_TRY(cudaStreamSynchronize(b->stream));
-    for (int i = 0; i < b->count; ++i) {
-        const int st = apply_status(b->plans[i]);
-        if (st != NFFT2D_OK) return st;
+    // one launch bins every transform when their cell counters fit in shared
+    // memory (one CTA per transform); otherwise every transform's binning is
+    // enqueued without a host round trip and the status words (work-item
+    // counts, errors) of all of them come back with one synchronisation
+    {
+        std::vector<long long> Mi(b->count);
+        std::vector<const void *> px(b->count), py(b->count);
+        for (int i = 0; i < b->count; ++i) {  // internal order; the arguments are in the caller's
+            const int t = b->order[i];
+            Mi[i] = M[t];
+            px[i] = x1[t];
+            py[i] = x2[t];
+        }
+        int st = bin_small_batch(b->plans.data(), Mi.data(), px.data(), py.data(), coord_dtype, units, b->count,
+                                 b->stream);
+        if (st == NFFT2D_ERR_UNSUPPORTED) {
+            for (int i = 0; i < b->count; ++i) {
+                st = nfft2d_set_points_async(b->plans[i], Mi[i], px[i], py[i], coord_dtype, units);
+                if (st != NFFT2D_OK) return st;
+            }
+            for (int i = 0; i < b->count; ++i)
+                B_TRY(cudaMemcpyAsync(b->plans[i]->h_status, b->plans[i]->d_status, 4 * sizeof(int),
+                                      cudaMemcpyDeviceToHost, b->stream));
+            B_TRY(cudaStreamSynchronize(b->stream));
+            for (int i = 0; i < b->count; ++i)
+                if ((st = apply_status(b->plans[i])) != NFFT2D_OK) return st;
+        } else if (st != NFFT2D_OK) {
+            return st;
+        }
     }
     std::vector<BatchDesc> h(b->count);
     int chunks = 0, rows = 0, crop = 0;

@@ -210,6 +210,33 @@ cufftResult pooled_plan_many(cufftHandle *out, int rank, const int *n, const int
 cufftResult pooled_plan_2d(cufftHandle *out, int nx, int ny, cufftType type);
 void pooled_plan_release(cufftHandle h);
 
+// One transform's binning job for bin_small_batch (device copy).
+struct SmallBinJob {
+    const void *x1, *x2;  // DEVICE coordinates (FP32 or FP64 as the batch's call)
+    int M;
+    double s1, s2;        // sigma * unit scale per dimension
+    float s1f, s2f;
+    int exact;            // exact FP32 reduction (power-of-two scales, FP32 data)
+    Geom g;
+    Rec32 *tmp;           // the plan's buffers
+    uint2 *keyrank;
+    Rec32 *recs;
+    int *src;
+    int4 *chunks;
+    int chunk;
+    int *status;          // the plan's status words ([0] work items, [1] error bits)
+    int *out;             // work items and error bits, read back by the host
+};
+
+// Bin the points of `count` FP32 plans (a batch's transforms) with one
+// launch: one CTA per transform with its cell counters in shared memory.
+// Same result as nfft2d_set_points on each plan (units: NFFT2D_UNITS_*);
+// synchronizes once.  NFFT2D_ERR_UNSUPPORTED when a plan's cells
+// do not fit in shared memory or a transform has more than 2^24 points
+// (the caller bins those per plan).
+int bin_small_batch(nfft2d_plan_s *const *plans, const long long *M, const void *const *x1,
+                    const void *const *x2, int coord_dtype, int units, int count, cudaStream_t stream);
+
 // After the plan's status words were copied to p->h_status and its stream
 // went idle: completes a set_points enqueued by nfft2d_set_points_async
 // (the work-item count) and reports, then clears, the latched device-side

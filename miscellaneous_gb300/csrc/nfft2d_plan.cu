@@ -624,6 +624,17 @@ __device__ __forceinline__ bool reduce_coord(CT x, double o, double s, float sf,
     return true;
 }
 
+// Cell key of wrapped cell (mu1, mu2): tile, then strip, row and column
+// within the strip (row-major within the tile when the strip width is the
+// tile's).
+__device__ __forceinline__ unsigned cell_key(const Geom &g, int mu1, int mu2) {
+    const int tr = mu1 / g.T, tc = mu2 / g.T;
+    const int lr = mu1 - tr * g.T, lc = mu2 - tc * g.T;
+    const int st = lc / g.SW, sc = lc - st * g.SW;
+    return static_cast<unsigned>(tr * g.tiles2 + tc) * static_cast<unsigned>(g.T * g.T) +
+           static_cast<unsigned>((st * g.T + lr) * g.SW + sc);
+}
+
 template <typename CT, typename RecT>
 __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double o1, double o2,
                             double s1, double s2, float s1f, float s2f, int exact_f32, Geom g, RecT *__restrict__ tmp,
@@ -646,12 +657,7 @@ __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2
         mu1 = mu2 = 0;
         r.t1 = r.t2 = 0;
     }
-    // cell key: tile, then strip, row and column within the strip
-    const int tr = mu1 / g.T, tc = mu2 / g.T;
-    const int lr = mu1 - tr * g.T, lc = mu2 - tc * g.T;
-    const int st = lc / g.SW, sc = lc - st * g.SW;
-    const unsigned key = static_cast<unsigned>(tr * g.tiles2 + tc) * static_cast<unsigned>(g.T * g.T) +
-                         static_cast<unsigned>((st * g.T + lr) * g.SW + sc);
+    const unsigned key = cell_key(g, mu1, mu2);
     const unsigned rank = atomicAdd(cell_count + key, 1u);
     r.mu = (mu1 << 16) | mu2;
     r.orig = i;
@@ -679,6 +685,120 @@ __global__ void k_bin_gather(const RecT *__restrict__ tmp, const int *__restrict
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= M) return;
     recs[q] = tmp[__ldg(src + q)];
+}
+
+// ---------------------------------------------------------------------------
+// Binning of many small point sets at once (the transforms of a batch): one
+// 1024-thread CTA per transform does the whole counting sort with its cell
+// counters in shared memory -- reduction, key and rank (shared atomics),
+// scan, ordered records, work items -- so a batch of hundreds of small
+// transforms bins in one launch instead of five launches and two memsets
+// each.  Same records, keys and work items as the per-plan binning.
+// ---------------------------------------------------------------------------
+constexpr int kSmallBinThreads = 1024;
+
+// Exclusive block-wide scan of one value per thread; *total gets the sum.
+__device__ unsigned small_block_scan(unsigned v, unsigned *warp_sums, unsigned *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = warp_sums[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const unsigned excl = (warp ? warp_sums[warp - 1] : 0u) + incl - v;
+    if (total) *total = warp_sums[31];
+    __syncthreads();  // warp_sums reusable
+    return excl;
+}
+
+template <typename CT>
+__global__ void __launch_bounds__(kSmallBinThreads, 1) k_bin_small(const SmallBinJob *__restrict__ jobs) {
+    extern __shared__ unsigned sb_smem[];
+    const SmallBinJob J = jobs[blockIdx.x];
+    const Geom &g = J.g;
+    const int ncells = g.tiles1 * g.tiles2 * g.T * g.T;
+    unsigned *cnt = sb_smem;                 // ncells + 1 counters, then the exclusive starts
+    unsigned *ws = sb_smem + ncells + 1;     // 32 warp sums
+    const int tid = threadIdx.x;
+    for (int i = tid; i <= ncells; i += kSmallBinThreads) cnt[i] = 0u;
+    if (tid < 4) J.status[tid] = 0;  // a new point set: no work items, no error bits
+    __syncthreads();
+    const CT *x1 = static_cast<const CT *>(J.x1), *x2 = static_cast<const CT *>(J.x2);
+    bool bad = false;
+    for (int i = tid; i < J.M; i += kSmallBinThreads) {
+        Rec32 r;
+        int mu1, mu2;
+        const bool ok1 = reduce_coord(x1[i], 0.0, J.s1, J.s1f, J.exact != 0, g.n1, mu1, r.t1);
+        const bool ok2 = reduce_coord(x2[i], 0.0, J.s2, J.s2f, J.exact != 0, g.n2, mu2, r.t2);
+        if (!ok1 || !ok2) {  // as k_bin_pass1: reported, and binned at cell 0 with t = 0
+            bad = true;
+            mu1 = mu2 = 0;
+            r.t1 = r.t2 = 0.f;
+        }
+        const unsigned key = cell_key(g, mu1, mu2);
+        r.mu = (mu1 << 16) | mu2;
+        r.orig = i;
+        J.tmp[i] = r;
+        J.keyrank[i] = make_uint2(key, atomicAdd(cnt + key, 1u));
+    }
+    if (bad) atomicOr(J.status + 1, kErrNonfinite);
+    __syncthreads();
+    // exclusive scan of the counters: each thread sums a contiguous run
+    const int per = (ncells + 1 + kSmallBinThreads - 1) / kSmallBinThreads;
+    const int c0 = min(tid * per, ncells + 1), c1 = min(c0 + per, ncells + 1);
+    unsigned run = 0;
+    for (int c = c0; c < c1; ++c) run += cnt[c];
+    unsigned base = small_block_scan(run, ws, nullptr);
+    for (int c = c0; c < c1; ++c) {
+        const unsigned v = cnt[c];
+        cnt[c] = base;
+        base += v;
+    }
+    __syncthreads();
+    // records in cell order and the permutation
+    for (int i = tid; i < J.M; i += kSmallBinThreads) {
+        const uint2 kr = J.keyrank[i];
+        const unsigned q = cnt[kr.x] + kr.y;
+        J.recs[q] = J.tmp[i];
+        J.src[q] = i;
+    }
+    // work items: per tile, ceil(count / chunk) items of at most chunk points
+    const int ntiles = g.tiles1 * g.tiles2, cpt = g.T * g.T;
+    unsigned items_before = 0;
+    for (int t0 = 0; t0 < ntiles; t0 += kSmallBinThreads) {
+        const int t = t0 + tid;
+        unsigned start = 0, count = 0, items = 0;
+        if (t < ntiles) {
+            start = cnt[t * cpt];
+            count = cnt[(t + 1) * cpt] - start;  // cnt[ncells] is M
+            items = (count + J.chunk - 1) / J.chunk;
+        }
+        unsigned total = 0;
+        const unsigned at = items_before + small_block_scan(items, ws, &total);
+        for (unsigned c = 0; c < items; ++c) {
+            const unsigned off = c * J.chunk;
+            J.chunks[at + c] = make_int4(t, static_cast<int>(start + off),
+                                         static_cast<int>(min(count - off, static_cast<unsigned>(J.chunk))), 0);
+        }
+        items_before += total;
+    }
+    if (tid == 0) {
+        J.status[0] = static_cast<int>(items_before);
+        J.out[0] = static_cast<int>(items_before);
+    }
+    __syncthreads();
+    if (tid == 0) J.out[1] = J.status[1];
 }
 
 // ---------------------------------------------------------------------------
@@ -1549,6 +1669,103 @@ static int coord_device_ptr(const nfft2d_plan_s *p, const void *x, const void **
 }
 
 extern "C++" {
+int nfft2d::bin_small_batch(nfft2d_plan_s *const *plans, const long long *M, const void *const *x1,
+                             const void *const *x2, int coord_dtype, int units, int count, cudaStream_t stream) {
+    if (count < 1 || (coord_dtype != NFFT2D_COORD_F32 && coord_dtype != NFFT2D_COORD_F64))
+        return NFFT2D_ERR_INVALID_ARG;
+    if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
+        return NFFT2D_ERR_INVALID_ARG;
+    std::vector<SmallBinJob> jobs(static_cast<size_t>(count));
+    size_t max_cells = 0;
+    for (int i = 0; i < count; ++i) {
+        nfft2d_plan_s *p = plans[i];
+        if (!p || M[i] < 0 || M[i] > (1LL << 24) || p->precision != NFFT2D_F32) return NFFT2D_ERR_UNSUPPORTED;
+        if (M[i] > 0 && (!x1[i] || !x2[i])) return NFFT2D_ERR_INVALID_ARG;
+        max_cells = std::max(max_cells, p->ncells);
+    }
+    const size_t smem = sizeof(unsigned) * (max_cells + 1 + 32);
+    if (smem > 200 * 1024) return NFFT2D_ERR_UNSUPPORTED;  // the counters must fit in shared memory
+    int *d_out = nullptr;
+    SmallBinJob *d_jobs = nullptr;
+    for (int i = 0; i < count; ++i) {
+        nfft2d_plan_s *p = plans[i];
+        const void *dx1 = x1[i], *dx2 = x2[i];
+        if (M[i] > 0) {
+            int st = coord_device_ptr(p, x1[i], &dx1);
+            if (st == NFFT2D_OK) st = coord_device_ptr(p, x2[i], &dx2);
+            if (st != NFFT2D_OK) return st;
+        }
+        p->points_valid = false;
+        p->M = 0;
+        p->n_chunks = 0;
+        const int st = ensure_points_capacity(p, std::max<long long>(M[i], 1));
+        if (st != NFFT2D_OK) return st;
+        p->workspace_bytes = plan_workspace_bytes(p);
+        // the unit scales of nfft2d_set_points
+        const double u1 = units == NFFT2D_UNITS_GRID ? 1.0 : (units == NFFT2D_UNITS_UNIT ? p->N1 : p->N1 / (2.0 * kPi));
+        const double u2 = units == NFFT2D_UNITS_GRID ? 1.0 : (units == NFFT2D_UNITS_UNIT ? p->N2 : p->N2 / (2.0 * kPi));
+        const double s1 = p->sigma * u1, s2 = p->sigma * u2;
+        p->xscale1 = s1;
+        p->xscale2 = s2;
+        int e1 = 0, e2 = 0;
+        const bool pow2 = std::frexp(s1, &e1) == 0.5 && std::frexp(s2, &e2) == 0.5;
+        SmallBinJob &J = jobs[static_cast<size_t>(i)];
+        J.x1 = dx1;
+        J.x2 = dx2;
+        J.M = static_cast<int>(M[i]);
+        J.s1 = s1;
+        J.s2 = s2;
+        J.s1f = static_cast<float>(s1);
+        J.s2f = static_cast<float>(s2);
+        J.exact = (coord_dtype == NFFT2D_COORD_F32 && pow2) ? 1 : 0;
+        J.g = p->g;
+        J.tmp = static_cast<Rec32 *>(p->tmp_recs);
+        J.keyrank = p->keyrank;
+        J.recs = static_cast<Rec32 *>(p->recs);
+        J.src = p->src;
+        J.chunks = p->chunks;
+        J.chunk = p->chunk;
+        J.status = p->d_status;
+        J.out = nullptr;  // set below
+    }
+    NFFT_TRY_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&d_out), sizeof(int) * 2 * count, stream));
+    for (int i = 0; i < count; ++i) jobs[static_cast<size_t>(i)].out = d_out + 2 * i;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&d_jobs), sizeof(SmallBinJob) * count, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SmallBinJob) * count, cudaMemcpyHostToDevice, stream);
+    auto kernel = coord_dtype == NFFT2D_COORD_F64 ? k_bin_small<double> : k_bin_small<float>;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e == cudaSuccess) {
+        kernel<<<count, kSmallBinThreads, smem, stream>>>(d_jobs);
+        e = cudaGetLastError();
+    }
+    std::vector<int> out(static_cast<size_t>(2 * count));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out.data(), d_out, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    cudaFreeAsync(d_jobs, stream);
+    cudaFreeAsync(d_out, stream);
+    if (e != cudaSuccess) return status_from_cuda(e);
+    int status = NFFT2D_OK;
+    for (int i = 0; i < count; ++i) {
+        nfft2d_plan_s *p = plans[i];
+        const int n_chunks = out[static_cast<size_t>(2 * i)], bits = out[static_cast<size_t>(2 * i + 1)];
+        if (bits & kErrNonfinite) {
+            status = NFFT2D_ERR_NONFINITE;
+            continue;
+        }
+        if (n_chunks < 0 || n_chunks > p->chunks_cap) return NFFT2D_ERR_INTERNAL;
+        p->M = M[i];
+        p->n_chunks = n_chunks;
+        p->points_valid = true;
+        if (p->gather_auto) p->gather_variant = auto_gather(p, M[i]);
+    }
+    if (status != NFFT2D_OK)  // the error bits are reported here, not again by synchronize
+        for (int i = 0; i < count; ++i) cudaMemsetAsync(plans[i]->d_status + 1, 0, sizeof(int), stream);
+    return status;
+}
+
 int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype,
                               double u1, double u2, double o1, double o2, bool async) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;

@@ -139,3 +139,26 @@ def test_uneven_window_widths_in_one_batch(orc, graph):
             assert orc.rel_l2(got_f, orc.ndft_type2(F, g1, g2, sign=-1)) < bar, t
             exact_F = orc.ndft_type1(f.astype(np.complex128), g1, g2, n1, n2, sign=+1)
             assert orc.rel_l2(got_F.reshape(n1, n2), exact_F) < bar, t
+
+
+def test_batch_binning_reports_nonfinite_then_recovers(orc):
+    """The batched binning (one CTA per transform) reports a NaN coordinate as
+    NFFT2D_ERR_NONFINITE, like nfft2d_set_points, and the batch bins
+    correctly afterwards."""
+    from miscellaneous_gb300 import _lib
+    from miscellaneous_gb300.nfft import Batch
+    sizes = [(32, 32), (48, 32), (32, 32)]
+    Ms = [500, 700, 300]
+    xs, Fs, _ = _problem(sizes, Ms, 21)
+    bad = [(x[0].copy(), x[1].copy()) for x in xs]
+    bad[1][0][17] = np.nan
+    with Batch(sizes) as bt:
+        with pytest.raises(_lib.NFFT2DError) as e:
+            bt.set_points([torch.from_numpy(x[0]).cuda() for x in bad], [torch.from_numpy(x[1]).cuda() for x in bad])
+        assert e.value.status == _lib.ERR_NONFINITE
+        bt.set_points([torch.from_numpy(x[0]).cuda() for x in xs], [torch.from_numpy(x[1]).cuda() for x in xs])
+        outs = bt.forward([torch.from_numpy(F).cuda().reshape(-1) for F in Fs])
+        bt.synchronize()
+        for t, ((n1, n2), x, F) in enumerate(zip(sizes, xs, Fs)):
+            g1, g2 = x[0].astype(np.float64) * n1, x[1].astype(np.float64) * n2
+            assert orc.rel_l2(outs[t].cpu().numpy(), orc.ndft_type2(F, g1, g2, sign=-1)) < 1e-5, t

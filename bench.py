@@ -918,17 +918,19 @@ def run_ours(args, wl):
         def e2e_step():
             dF.copy_(hF, non_blocking=True)
             if mode["direct"]:
-                plan.set_points(hx1, hx2, units="unit", sync=False)
+                cx1, cx2 = hx1, hx2
             else:
                 dx1.copy_(hx1, non_blocking=True)
                 dx2.copy_(hx2, non_blocking=True)
-                plan.set_points(dx1, dx2, units="unit", sync=False)
-            ev_sp.record(stream)
+                cx1, cx2 = dx1, dx2
+            # binning + forward in one call: the forward's pad and FFT run
+            # while the points are binned; ev_sp marks the coordinates read,
+            # after which f goes up on the second stream
+            plan.bin_and_forward(cx1, cx2, dF, units="unit", out=f_out, coords_read=ev_sp)
             cs.wait_event(ev_sp)
             with torch.cuda.stream(cs):
                 df.copy_(hf, non_blocking=True)
                 ev_in.record(cs)
-            sharded.forward(dF, out=f_out)
             ev_fwd.record(stream)
             stream.wait_event(ev_in)
             sharded.adjoint(df, out=F_out)
@@ -998,11 +1000,11 @@ def run_ours(args, wl):
                "coords_upload_ms": cu, "coords_upload_gbs": (hx1.numel() + hx2.numel()) * 4 / (cu * 1e-3) / 1e9,
                "coords": "direct" if mode["direct"] else "copy", "coords_trial_ms": trial,
                "includes": "H2D of F, the coordinates (read by the binning pass over the link with coords "
-                           "'direct', copied first with 'copy'; the faster of the two in an untimed trial) and f, set_points (binning sort, enqueued "
-                           "without a host round trip), forward, adjoint, D2H of f_out and F_out; f goes up "
-                           "during the binning's tail and the forward, f_out comes down during the adjoint "
-                           "(second stream); the plan status is read and L2 is flushed (256 MB written) after "
-                           "each step, outside the events"}
+                           "'direct', copied first with 'copy'; the faster of the two in an untimed trial) and f; "
+                           "binning + forward in one call (nfft2d_bin_and_forward: the forward's pad and FFT run "
+                           "while the points are binned), adjoint, D2H of f_out and F_out; f goes up once the "
+                           "coordinates are read, f_out comes down during the adjoint (second stream); the plan "
+                           "status is read and L2 is flushed (256 MB written) after each step, outside the events"}
         # restore the resident plan state for the accuracy check
         plan.set_points(x1, x2, units="unit")
 

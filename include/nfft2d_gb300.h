@@ -195,6 +195,17 @@ int nfft2d_set_points(nfft2d_plan plan, long long M, const void *x1, const void 
 int nfft2d_set_points_async(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype,
                             int units);
 
+/* nfft2d_set_points_async followed by nfft2d_forward (type 2, sign -1) in one
+ * call, with the same result: the forward's padding and FFT, which read only
+ * F, run on a second stream while the binning reads the coordinates (from
+ * page-locked host memory over the host link, or from the device) and sorts
+ * them; the gather follows both on the plan's stream.  coords_read_event
+ * (a cudaEvent_t, or NULL) is recorded once the coordinates have been read:
+ * their buffers and the host link are free from there (e.g. to upload the
+ * next inputs).  Not for plans of a batch.  No reference counterpart. */
+int nfft2d_bin_and_forward(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype, int units,
+                           const void *F, void *f, void *coords_read_event);
+
 /* ---- transforms ---------------------------------------------------------
  * nfft2d_forward   : type 2, sign -1  (BP_FBP_FFBP/NFFT1_2D.m:1-69)
  * nfft2d_adjoint   : type 1, sign +1  (Hermitian adjoint of nfft2d_forward)

@@ -119,6 +119,7 @@ _SIGNATURES = {
     "nfft2d_layout_query": (_I, [_I, _I, _D, _I, _I, _I, ctypes.POINTER(Info)]),
     "nfft2d_set_points": (_I, [_P, _LL, _P, _P, _I, _I]),
     "nfft2d_set_points_async": (_I, [_P, _LL, _P, _P, _I, _I]),
+    "nfft2d_bin_and_forward": (_I, [_P, _LL, _P, _P, _I, _I, _P, _P, _P]),
     "nfft2d_forward": (_I, [_P, _P, _P]),
     "nfft2d_adjoint": (_I, [_P, _P, _P]),
     "nfft2d_spread_ref": (_I, [_P, _P, _P]),

@@ -138,6 +138,8 @@ struct nfft2d_plan_s {
     double xscale1 = 1.0, xscale2 = 1.0;  // dt/dx for the units given to set_points
 
     bool strips = true;  // strip-major cell order (false: row-major, a gather-only plan)
+    cudaStream_t aux = nullptr;                         // second stream of nfft2d_bin_and_forward
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // its fork and join
     cufftHandle fft = 0;
     bool fft_ok = false;
     cufftHandle fft_rows = 0, fft_cols = 0;  // pruned 1D passes (see run_fft)
@@ -192,9 +194,11 @@ int tensor_map_for(nfft2d_plan_s *p);
 // Bin points whose grid-unit coordinates are (x - o) * u per dimension (the
 // public set_points uses o = 0 and u from its units argument).  async: return
 // after enqueuing; the work-item count stays on the device (n_chunks = -1)
-// until nfft2d_synchronize reads it back with the error bits.
+// until nfft2d_synchronize reads it back with the error bits.  coords_read,
+// if given, is recorded once the coordinates have been read (their buffers
+// and the host link are free from there).
 int set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype, double u1,
-                      double u2, double o1, double o2, bool async = false);
+                      double u2, double o1, double o2, bool async = false, cudaEvent_t coords_read = nullptr);
 
 // cuFFT plans from a process-wide pool keyed by the device and every plan
 // parameter: creating a plan of an awkward size costs milliseconds (a

@@ -1004,6 +1004,12 @@ void release_ffts(nfft2d_plan_s *p) {
 void destroy_plan(nfft2d_plan_s *p) {
     if (!p) return;
     cudaStreamSynchronize(p->stream);  // its buffers go back to the cache: nothing of the plan in flight
+    if (p->aux) {
+        cudaStreamSynchronize(p->aux);
+        cudaStreamDestroy(p->aux);
+    }
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
     release_ffts(p);
     free_points(p);
     if (!p->grid_external) plan_free(p->grid);
@@ -1767,7 +1773,7 @@ int nfft2d::bin_small_batch(nfft2d_plan_s *const *plans, const long long *M, con
 }
 
 int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, const void *x2, int coord_dtype,
-                              double u1, double u2, double o1, double o2, bool async) {
+                              double u1, double u2, double o1, double o2, bool async, cudaEvent_t coords_read) {
     if (!p) return NFFT2D_ERR_INVALID_ARG;
     if (M < 0 || M > 0x7fffffffLL) return NFFT2D_ERR_INVALID_ARG;
     if (coord_dtype != NFFT2D_COORD_F32 && coord_dtype != NFFT2D_COORD_F64) return NFFT2D_ERR_INVALID_ARG;
@@ -1789,6 +1795,7 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     p->workspace_bytes = plan_workspace_bytes(p);
     if (M == 0) {
         p->points_valid = true;
+        if (coords_read) NFFT_TRY_CUDA(cudaEventRecord(coords_read, p->stream));
         return NFFT2D_OK;
     }
     const Geom &g = p->g;
@@ -1830,6 +1837,7 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
                 static_cast<Rec32 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
     }
     NFFT_TRY_CUDA(cudaGetLastError());
+    if (coords_read) NFFT_TRY_CUDA(cudaEventRecord(coords_read, p->stream));  // the coordinates are read
     const size_t cells_n = p->ncells + 1;
     k_scan_counts<<<static_cast<unsigned>((cells_n + kCellTile - 1) / kCellTile), kCellScanThreads, 0, p->stream>>>(
         p->cell_count, cells_n, scan_state, p->d_status);
@@ -1955,6 +1963,53 @@ int nfft2d_set_points(nfft2d_plan p, long long M, const void *x1, const void *x2
 
 int nfft2d_set_points_async(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units) {
     return nfft2d_set_points_impl(p, M, x1, x2, coord_dtype, units, true);
+}
+
+// nfft2d_set_points_async + nfft2d_forward, with the forward's padding and
+// FFT (which read only F and the grid) on a second stream forked before the
+// binning, so they run while the binning's first pass reads the coordinates
+// (over the host link, for page-locked host coordinates) and the rest of the
+// binning runs; the gather waits for both.
+int nfft2d_bin_and_forward(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units,
+                           const void *F, void *f, void *coords_read_event) {
+    if (!p || !F || (M > 0 && !f)) return NFFT2D_ERR_INVALID_ARG;
+    if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
+        return NFFT2D_ERR_INVALID_ARG;
+    if (p->grid_external) return NFFT2D_ERR_UNSUPPORTED;  // batch plans: the batch runs the FFTs
+    const double u1 = units == NFFT2D_UNITS_GRID ? 1.0 : (units == NFFT2D_UNITS_UNIT ? p->N1 : p->N1 / (2.0 * kPi));
+    const double u2 = units == NFFT2D_UNITS_GRID ? 1.0 : (units == NFFT2D_UNITS_UNIT ? p->N2 : p->N2 / (2.0 * kPi));
+    if (!p->aux) NFFT_TRY_CUDA(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
+    if (!p->ev_fork) NFFT_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+    if (!p->ev_join) NFFT_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+    const cudaStream_t main = p->stream;
+    NFFT_TRY_CUDA(cudaEventRecord(p->ev_fork, main));
+    NFFT_TRY_CUDA(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
+    // pad + FFT (+ halo fill) on the second stream: every launch of the
+    // plan goes to p->stream, and the cuFFT plans to their bound stream
+    auto bind = [&](cudaStream_t s) {
+        p->stream = s;
+        if (p->fft_ok) cufftSetStream(p->fft, s);
+        if (p->pruned_ok) {
+            cufftSetStream(p->fft_rows, s);
+            cufftSetStream(p->fft_cols, s);
+        }
+    };
+    timer_reset(p, CALL_TYPE2);
+    bind(p->aux);
+    int st = type2_prepare(p, -1, F);  // NFFT1_2D.m: exp(-i)
+    bind(main);
+    if (st != NFFT2D_OK) return st;
+    NFFT_TRY_CUDA(cudaEventRecord(p->ev_join, p->aux));
+    st = nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0, true,
+                                   static_cast<cudaEvent_t>(coords_read_event));
+    // the grid is the padded, transformed F from here on, whatever happened
+    NFFT_TRY_CUDA(cudaStreamWaitEvent(main, p->ev_join, 0));
+    if (st != NFFT2D_OK) return st;
+    if (M == 0) return NFFT2D_OK;
+    stage_begin(p, ST_GATHER);
+    NFFT_TRY_CUDA(launch_gather(p, f));
+    stage_end(p, ST_GATHER);
+    return NFFT2D_OK;
 }
 
 int nfft2d_type2(nfft2d_plan p, int sign, const void *F, void *f) {

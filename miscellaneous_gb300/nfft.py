@@ -162,6 +162,36 @@ class Plan:
         self.M = M
         self._keep = (x1, x2)
 
+    def bin_and_forward(self, x1: torch.Tensor, x2: torch.Tensor, F: torch.Tensor, units: str = "unit",
+                        out: torch.Tensor | None = None, coords_read: torch.cuda.Event | None = None) -> torch.Tensor:
+        """set_points(x1, x2, sync=False) then forward(F), with the forward's
+        padding and FFT running while the points are binned (they read only
+        F).  coords_read, a torch.cuda.Event, is recorded once the coordinates
+        have been read (their buffers and the host link are free from there)."""
+        if x1.shape != x2.shape or x1.dim() != 1:
+            raise ValueError("x1 and x2 must be 1-D tensors of equal length")
+        if x1.dtype not in (torch.float32, torch.float64) or x2.dtype != x1.dtype:
+            raise TypeError("coordinates must both be float32 or both float64")
+        for t, name in ((x1, "x1"), (x2, "x2")):
+            if t.is_cuda:
+                _require_cuda(t, name, x1.dtype)
+            elif not (t.is_pinned() and t.is_contiguous()):
+                raise TypeError(f"{name} must be a CUDA tensor or a contiguous pinned CPU tensor")
+        F = self._coef(F)
+        M = x1.numel()
+        out = torch.empty(M, dtype=self.cdtype, device=F.device) if out is None else _require_cuda(
+            out, "out", self.cdtype, M)
+        ev = None
+        if coords_read is not None:
+            coords_read.record(self.stream)  # creates the event; the library records it again at the right point
+            ev = ctypes.c_void_p(coords_read.cuda_event)
+        cd = _lib.COORD_F32 if x1.dtype == torch.float32 else _lib.COORD_F64
+        check(self._lib.nfft2d_bin_and_forward(self._h, M, _ptr(x1), _ptr(x2), cd, _lib.UNITS[units], _ptr(F),
+                                               _ptr(out), ev), "nfft2d_bin_and_forward")
+        self.M = M
+        self._keep = (x1, x2)
+        return out
+
     # -- transforms ---------------------------------------------------------
     def _coef(self, F: torch.Tensor, name: str = "F") -> torch.Tensor:
         F = _require_cuda(F, name, self.cdtype, self.N1 * self.N2)

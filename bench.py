@@ -901,32 +901,34 @@ def run_ours(args, wl):
         hf_out = torch.empty(M, dtype=torch.complex64).pin_memory()
         hF_out = torch.empty(N1 * N2, dtype=torch.complex64).pin_memory()
         dx1, dx2 = torch.empty_like(x1), torch.empty_like(x2)
-        dF, df = torch.empty_like(F), torch.empty_like(f)
+        df = torch.empty_like(f)
         plan.enable_timing(False)
         # The link carries x1, x2, F and f up and f_out, F_out down.  The
-        # binning needs the coordinates first and the forward needs F, so
-        # those go first and alone (concurrent uploads share the link); f
-        # goes up on a second stream while the binning finishes and the
-        # forward runs, and f_out comes down on it while the adjoint runs.
-        # e2e_coords "direct": the binning pass reads the page-locked
-        # coordinates over the link itself (set_points accepts them), so the
-        # upload and the pass overlap; "copy": they are copied first.
+        # binning needs the coordinates first, so they go first and alone
+        # (concurrent uploads share the link); the library uploads the
+        # page-locked F once they are read, while the rest of the binning
+        # runs; f goes up on a second stream once those inputs are read,
+        # while the forward runs, and f_out comes down on it while the
+        # adjoint runs.  e2e_coords "direct": the binning pass reads the
+        # page-locked coordinates over the link itself (set_points accepts
+        # them), so the upload and the pass overlap; "copy": they are
+        # copied first.
         cs = torch.cuda.Stream(device=dev)
         ev_sp, ev_in, ev_fwd, ev_out = (torch.cuda.Event() for _ in range(4))
         mode = {"direct": args.e2e_coords == "direct"}
 
         def e2e_step():
-            dF.copy_(hF, non_blocking=True)
             if mode["direct"]:
                 cx1, cx2 = hx1, hx2
             else:
                 dx1.copy_(hx1, non_blocking=True)
                 dx2.copy_(hx2, non_blocking=True)
                 cx1, cx2 = dx1, dx2
-            # binning + forward in one call: the forward's pad and FFT run
-            # while the points are binned; ev_sp marks the coordinates read,
-            # after which f goes up on the second stream
-            plan.bin_and_forward(cx1, cx2, dF, units="unit", out=f_out, coords_read=ev_sp)
+            # binning + forward in one call: F goes up once the coordinates
+            # are read, and the forward's pad and FFT run while the points
+            # are binned; ev_sp marks the inputs read, after which f goes up
+            # on the second stream
+            plan.bin_and_forward(cx1, cx2, hF, units="unit", out=f_out, inputs_read=ev_sp)
             cs.wait_event(ev_sp)
             with torch.cuda.stream(cs):
                 df.copy_(hf, non_blocking=True)
@@ -999,12 +1001,13 @@ def run_ours(args, wl):
                "d2h_bytes_per_step": d2h, "ms_per_step": te,
                "coords_upload_ms": cu, "coords_upload_gbs": (hx1.numel() + hx2.numel()) * 4 / (cu * 1e-3) / 1e9,
                "coords": "direct" if mode["direct"] else "copy", "coords_trial_ms": trial,
-               "includes": "H2D of F, the coordinates (read by the binning pass over the link with coords "
-                           "'direct', copied first with 'copy'; the faster of the two in an untimed trial) and f; "
-                           "binning + forward in one call (nfft2d_bin_and_forward: the forward's pad and FFT run "
-                           "while the points are binned), adjoint, D2H of f_out and F_out; f goes up once the "
-                           "coordinates are read, f_out comes down during the adjoint (second stream); the plan "
-                           "status is read and L2 is flushed (256 MB written) after each step, outside the events"}
+               "includes": "H2D of the coordinates (read by the binning pass over the link with coords "
+                           "'direct', copied first with 'copy'; the faster of the two in an untimed trial), F and f; "
+                           "binning + forward in one call (nfft2d_bin_and_forward with the page-locked F: F goes up "
+                           "once the coordinates are read, the forward's pad and FFT run while the points are "
+                           "binned), adjoint, D2H of f_out and F_out; f goes up once those inputs are read, f_out "
+                           "comes down during the adjoint (second stream); the plan status is read and L2 is "
+                           "flushed (256 MB written) after each step, outside the events"}
         # restore the resident plan state for the accuracy check
         plan.set_points(x1, x2, units="unit")
 

@@ -199,12 +199,18 @@ int nfft2d_set_points_async(nfft2d_plan plan, long long M, const void *x1, const
  * call, with the same result: the forward's padding and FFT, which read only
  * F, run on a second stream while the binning reads the coordinates (from
  * page-locked host memory over the host link, or from the device) and sorts
- * them; the gather follows both on the plan's stream.  coords_read_event
- * (a cudaEvent_t, or NULL) is recorded once the coordinates have been read:
- * their buffers and the host link are free from there (e.g. to upload the
- * next inputs).  Not for plans of a batch.  No reference counterpart. */
+ * them; the gather follows both on the plan's stream.  F may be device
+ * memory or page-locked host memory; from the host it is copied (into a
+ * device buffer the plan keeps) once the coordinates have been read, so the
+ * two uploads do not share the link and the copy overlaps the rest of the
+ * binning.  inputs_read_event (a cudaEvent_t, or NULL) is recorded once the
+ * call's inputs have been read -- the coordinates, and a host F -- so their
+ * buffers and the host link are free from there (e.g. to upload the next
+ * inputs).
+ * Pageable host memory returns NFFT2D_ERR_INVALID_ARG.  Not for plans of a
+ * batch.  No reference counterpart. */
 int nfft2d_bin_and_forward(nfft2d_plan plan, long long M, const void *x1, const void *x2, int coord_dtype, int units,
-                           const void *F, void *f, void *coords_read_event);
+                           const void *F, void *f, void *inputs_read_event);
 
 /* ---- transforms ---------------------------------------------------------
  * nfft2d_forward   : type 2, sign -1  (BP_FBP_FFBP/NFFT1_2D.m:1-69)

@@ -140,6 +140,9 @@ struct nfft2d_plan_s {
     bool strips = true;  // strip-major cell order (false: row-major, a gather-only plan)
     cudaStream_t aux = nullptr;                         // second stream of nfft2d_bin_and_forward
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // its fork and join
+    cudaEvent_t ev_coords = nullptr;                    // its coordinates-read mark
+    void *F_stage = nullptr;                            // its device copy of a host F
+    size_t F_stage_bytes = 0;
     cufftHandle fft = 0;
     bool fft_ok = false;
     cufftHandle fft_rows = 0, fft_cols = 0;  // pruned 1D passes (see run_fft)

@@ -1010,6 +1010,8 @@ void destroy_plan(nfft2d_plan_s *p) {
     }
     if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->ev_join) cudaEventDestroy(p->ev_join);
+    if (p->ev_coords) cudaEventDestroy(p->ev_coords);
+    plan_free(p->F_stage);
     release_ffts(p);
     free_points(p);
     if (!p->grid_external) plan_free(p->grid);
@@ -1966,24 +1968,52 @@ int nfft2d_set_points_async(nfft2d_plan p, long long M, const void *x1, const vo
 }
 
 // nfft2d_set_points_async + nfft2d_forward, with the forward's padding and
-// FFT (which read only F and the grid) on a second stream forked before the
-// binning, so they run while the binning's first pass reads the coordinates
-// (over the host link, for page-locked host coordinates) and the rest of the
-// binning runs; the gather waits for both.
+// FFT (which read only F and the grid) on a second stream, so they run while
+// the binning's first pass reads the coordinates (over the host link, for
+// page-locked host coordinates) and the rest of the binning runs; the gather
+// waits for both.  F in device memory: the second stream starts at once.  F
+// in page-locked host memory: it is copied into a staging buffer on the
+// second stream once the coordinates have been read, so the two uploads do
+// not share the link and F's copy overlaps the rest of the binning.
 int nfft2d_bin_and_forward(nfft2d_plan p, long long M, const void *x1, const void *x2, int coord_dtype, int units,
-                           const void *F, void *f, void *coords_read_event) {
+                           const void *F, void *f, void *inputs_read_event) {
     if (!p || !F || (M > 0 && !f)) return NFFT2D_ERR_INVALID_ARG;
     if (units != NFFT2D_UNITS_GRID && units != NFFT2D_UNITS_UNIT && units != NFFT2D_UNITS_RADIANS)
         return NFFT2D_ERR_INVALID_ARG;
     if (p->grid_external) return NFFT2D_ERR_UNSUPPORTED;  // batch plans: the batch runs the FFTs
+    cudaPointerAttributes fa;
+    if (cudaPointerGetAttributes(&fa, F) != cudaSuccess) {
+        cudaGetLastError();
+        return NFFT2D_ERR_INVALID_ARG;
+    }
+    const bool F_host = fa.type == cudaMemoryTypeHost;
+    if (!F_host && fa.type != cudaMemoryTypeDevice && fa.type != cudaMemoryTypeManaged)
+        return NFFT2D_ERR_INVALID_ARG;  // pageable host memory
+    const size_t F_bytes = static_cast<size_t>(p->N1) * p->N2 * (p->precision == NFFT2D_F64 ? 16 : 8);
     const double u1 = units == NFFT2D_UNITS_GRID ? 1.0 : (units == NFFT2D_UNITS_UNIT ? p->N1 : p->N1 / (2.0 * kPi));
     const double u2 = units == NFFT2D_UNITS_GRID ? 1.0 : (units == NFFT2D_UNITS_UNIT ? p->N2 : p->N2 / (2.0 * kPi));
     if (!p->aux) NFFT_TRY_CUDA(cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking));
     if (!p->ev_fork) NFFT_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
     if (!p->ev_join) NFFT_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+    if (!p->ev_coords) NFFT_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_coords, cudaEventDisableTiming));
+    if (F_host && p->F_stage_bytes < F_bytes) {
+        NFFT_TRY_CUDA(cudaStreamSynchronize(p->aux));  // the staging buffer's last reader
+        plan_free(p->F_stage);
+        p->F_stage = nullptr;
+        p->F_stage_bytes = 0;
+        NFFT_TRY_CUDA(plan_malloc(&p->F_stage, F_bytes));
+        p->F_stage_bytes = F_bytes;
+    }
     const cudaStream_t main = p->stream;
     NFFT_TRY_CUDA(cudaEventRecord(p->ev_fork, main));
     NFFT_TRY_CUDA(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
+    // inputs_read_event marks the host inputs read: the coordinates, and F
+    // too when it comes from the host (then recorded after F's copy)
+    const cudaEvent_t user_ev = static_cast<cudaEvent_t>(inputs_read_event);
+    const cudaEvent_t coords_read = (F_host || !user_ev) ? p->ev_coords : user_ev;
+    timer_reset(p, CALL_TYPE2);
+    int st = nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0, true, coords_read);
+    if (st != NFFT2D_OK) return st;
     // pad + FFT (+ halo fill) on the second stream: every launch of the
     // plan goes to p->stream, and the cuFFT plans to their bound stream
     auto bind = [&](cudaStream_t s) {
@@ -1994,17 +2024,19 @@ int nfft2d_bin_and_forward(nfft2d_plan p, long long M, const void *x1, const voi
             cufftSetStream(p->fft_cols, s);
         }
     };
-    timer_reset(p, CALL_TYPE2);
+    const void *Fd = F;
+    if (F_host) {
+        NFFT_TRY_CUDA(cudaStreamWaitEvent(p->aux, coords_read, 0));
+        NFFT_TRY_CUDA(cudaMemcpyAsync(p->F_stage, F, F_bytes, cudaMemcpyHostToDevice, p->aux));
+        if (user_ev) NFFT_TRY_CUDA(cudaEventRecord(user_ev, p->aux));
+        Fd = p->F_stage;
+    }
     bind(p->aux);
-    int st = type2_prepare(p, -1, F);  // NFFT1_2D.m: exp(-i)
+    st = type2_prepare(p, -1, Fd);  // NFFT1_2D.m: exp(-i)
     bind(main);
     if (st != NFFT2D_OK) return st;
     NFFT_TRY_CUDA(cudaEventRecord(p->ev_join, p->aux));
-    st = nfft2d::set_points_scaled(p, M, x1, x2, coord_dtype, u1, u2, 0.0, 0.0, true,
-                                   static_cast<cudaEvent_t>(coords_read_event));
-    // the grid is the padded, transformed F from here on, whatever happened
     NFFT_TRY_CUDA(cudaStreamWaitEvent(main, p->ev_join, 0));
-    if (st != NFFT2D_OK) return st;
     if (M == 0) return NFFT2D_OK;
     stage_begin(p, ST_GATHER);
     NFFT_TRY_CUDA(launch_gather(p, f));

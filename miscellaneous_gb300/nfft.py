@@ -163,11 +163,14 @@ class Plan:
         self._keep = (x1, x2)
 
     def bin_and_forward(self, x1: torch.Tensor, x2: torch.Tensor, F: torch.Tensor, units: str = "unit",
-                        out: torch.Tensor | None = None, coords_read: torch.cuda.Event | None = None) -> torch.Tensor:
+                        out: torch.Tensor | None = None, inputs_read: torch.cuda.Event | None = None) -> torch.Tensor:
         """set_points(x1, x2, sync=False) then forward(F), with the forward's
         padding and FFT running while the points are binned (they read only
-        F).  coords_read, a torch.cuda.Event, is recorded once the coordinates
-        have been read (their buffers and the host link are free from there)."""
+        F).  x1, x2 and F may be CUDA tensors or contiguous pinned CPU
+        tensors; a pinned F is uploaded after the coordinates have been read,
+        while the rest of the binning runs.  inputs_read, a torch.cuda.Event,
+        is recorded once the inputs have been read (the coordinates, and a
+        pinned F): their buffers and the host link are free from there."""
         if x1.shape != x2.shape or x1.dim() != 1:
             raise ValueError("x1 and x2 must be 1-D tensors of equal length")
         if x1.dtype not in (torch.float32, torch.float64) or x2.dtype != x1.dtype:
@@ -177,14 +180,22 @@ class Plan:
                 _require_cuda(t, name, x1.dtype)
             elif not (t.is_pinned() and t.is_contiguous()):
                 raise TypeError(f"{name} must be a CUDA tensor or a contiguous pinned CPU tensor")
-        F = self._coef(F)
+        if F.is_cuda:
+            F = self._coef(F)
+            dev = F.device
+        else:
+            if not (F.is_pinned() and F.is_contiguous()):
+                raise TypeError("F must be a CUDA tensor or a contiguous pinned CPU tensor")
+            if F.dtype != self.cdtype or F.numel() != self.N1 * self.N2:
+                raise ValueError(f"F must hold {self.N1 * self.N2} elements of {self.cdtype}")
+            dev = x1.device if x1.is_cuda else torch.device("cuda", torch.cuda.current_device())
         M = x1.numel()
-        out = torch.empty(M, dtype=self.cdtype, device=F.device) if out is None else _require_cuda(
+        out = torch.empty(M, dtype=self.cdtype, device=dev) if out is None else _require_cuda(
             out, "out", self.cdtype, M)
         ev = None
-        if coords_read is not None:
-            coords_read.record(self.stream)  # creates the event; the library records it again at the right point
-            ev = ctypes.c_void_p(coords_read.cuda_event)
+        if inputs_read is not None:
+            inputs_read.record(self.stream)  # creates the event; the library records it again at the right point
+            ev = ctypes.c_void_p(inputs_read.cuda_event)
         cd = _lib.COORD_F32 if x1.dtype == torch.float32 else _lib.COORD_F64
         check(self._lib.nfft2d_bin_and_forward(self._h, M, _ptr(x1), _ptr(x2), cd, _lib.UNITS[units], _ptr(F),
                                                _ptr(out), ev), "nfft2d_bin_and_forward")

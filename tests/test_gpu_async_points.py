@@ -90,13 +90,14 @@ def test_automatic_gather_follows_bin_density():
         p.synchronize()
 
 
+@pytest.mark.parametrize("host_F", [False, True])
 @pytest.mark.parametrize("host_coords", [False, True])
 @pytest.mark.parametrize("N,M", [(64, 4096), (512, 300000), (1024, 100000)])
-def test_bin_and_forward_matches_set_points_then_forward(N, M, host_coords):
+def test_bin_and_forward_matches_set_points_then_forward(N, M, host_coords, host_F):
     """nfft2d_bin_and_forward (the forward's padding and FFT on a second stream
     while the points are binned) gives the same result as set_points +
-    forward, with device or page-locked host coordinates; its event marks the
-    coordinates read, and the adjoint that follows sees the new points."""
+    forward, with device or page-locked host coordinates and F; its event
+    marks the inputs read, and the adjoint that follows sees the new points."""
     from miscellaneous_gb300.nfft import Plan
     x1, x2, F, f = _inputs(M, N, seed=N + 1)
     with Plan(N, N) as p:
@@ -108,13 +109,19 @@ def test_bin_and_forward_matches_set_points_then_forward(N, M, host_coords):
         y1, y2, _, _ = _inputs(M // 2 + 1, N, seed=7)
         p.set_points(y1, y2)
         c1, c2 = (x1.cpu().pin_memory(), x2.cpu().pin_memory()) if host_coords else (x1, x2)
+        cF = F.cpu().pin_memory() if host_F else F
         ev = torch.cuda.Event()
-        got_f = p.bin_and_forward(c1, c2, F, coords_read=ev)
+        got_f = p.bin_and_forward(c1, c2, cF, inputs_read=ev)
         ev.synchronize()
+        if host_F:
+            cF.zero_()  # the inputs are read: rewriting the host F changes nothing
         got_F = p.adjoint(f)
         p.synchronize()
         torch.testing.assert_close(got_f, want_f, rtol=0, atol=0)  # same kernels, same order of sums
         assert _rel(got_F, want_F) < 1e-6                           # the spread's reduce order varies
-        got0 = p.bin_and_forward(x1[:0], x2[:0], F)
+        got0 = p.bin_and_forward(x1[:0], x2[:0], F.cpu().pin_memory() if host_F else F)
         p.synchronize()
         assert got0.numel() == 0
+        if host_F:  # pageable host memory is refused
+            with pytest.raises(TypeError):
+                p.bin_and_forward(x1, x2, F.cpu())

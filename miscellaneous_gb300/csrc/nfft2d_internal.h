@@ -110,6 +110,7 @@ struct nfft2d_plan_s {
     int binned_io = 0;           // per-point arrays (f, v, g) in binned order, see nfft2d_tuning.io_order
     int device = 0;
     int num_sms = 0;
+    int l2_bytes = 0;
     cudaStream_t stream = nullptr;
 
     // device buffers owned by the plan

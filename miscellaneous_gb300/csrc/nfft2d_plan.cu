@@ -635,7 +635,30 @@ __device__ __forceinline__ unsigned cell_key(const Geom &g, int mu1, int mu2) {
            static_cast<unsigned>((st * g.T + lr) * g.SW + sc);
 }
 
-template <typename CT, typename RecT>
+// Loads and stores of arrays that each binning pass streams through once.
+// STREAM (set when the binning's arrays exceed L2): evict-first hints, so
+// that the tables the passes hit at random -- the cell counters and starts,
+// the inverse permutation -- stay in L2; else plain accesses, so that what
+// one pass writes is still in L2 for the next.
+template <bool STREAM, typename T>
+__device__ __forceinline__ T ld_once(const T *p) {
+    if constexpr (STREAM) return __ldcs(p);
+    else return *p;
+}
+template <bool STREAM, typename T>
+__device__ __forceinline__ void st_once(T *p, const T &v) {
+    if constexpr (STREAM) __stcs(p, v);
+    else *p = v;
+}
+template <bool STREAM, typename RecT>
+__device__ __forceinline__ void st_rec(RecT *p, const RecT &r) {
+    if constexpr (STREAM && sizeof(RecT) == 16)
+        __stcs(reinterpret_cast<int4 *>(p), *reinterpret_cast<const int4 *>(&r));
+    else
+        *p = r;
+}
+
+template <typename CT, typename RecT, bool STREAM>
 __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2, int M, double o1, double o2,
                             double s1, double s2, float s1f, float s2f, int exact_f32, Geom g, RecT *__restrict__ tmp,
                             uint2 *__restrict__ keyrank, unsigned *__restrict__ cell_count,
@@ -647,8 +670,8 @@ __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2
     if (i >= M) return;
     RecT r;
     int mu1, mu2;
-    const bool ok1 = reduce_coord(x1[i], o1, s1, s1f, exact_f32 != 0, g.n1, mu1, r.t1);
-    const bool ok2 = reduce_coord(x2[i], o2, s2, s2f, exact_f32 != 0, g.n2, mu2, r.t2);
+    const bool ok1 = reduce_coord(ld_once<STREAM>(x1 + i), o1, s1, s1f, exact_f32 != 0, g.n1, mu1, r.t1);
+    const bool ok2 = reduce_coord(ld_once<STREAM>(x2 + i), o2, s2, s2f, exact_f32 != 0, g.n2, mu2, r.t2);
     if (!ok1 || !ok2) {
         // the error is reported; the point is still binned (at cell 0, t = 0)
         // so every sorted record stays in bounds for transforms that an
@@ -661,30 +684,31 @@ __global__ void k_bin_pass1(const CT *__restrict__ x1, const CT *__restrict__ x2
     const unsigned rank = atomicAdd(cell_count + key, 1u);
     r.mu = (mu1 << 16) | mu2;
     r.orig = i;
-    tmp[i] = r;
-    keyrank[i] = make_uint2(key, rank);
+    st_rec<STREAM>(tmp + i, r);
+    st_once<STREAM>(keyrank + i, make_uint2(key, rank));
 }
 
 // The sorted position of every point, inverted: src[cell_start[key] + rank]
 // = i.  The 4-byte writes land in an array a quarter of the records' size,
 // which stays in L2 where the writes merge into whole lines.
+template <bool STREAM>
 __global__ void k_bin_invert(const uint2 *__restrict__ keyrank, const unsigned *__restrict__ cell_start, int M,
                              int *__restrict__ src) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
-    const uint2 kr = __ldg(keyrank + i);
+    const uint2 kr = ld_once<STREAM>(keyrank + i);
     src[cell_start[kr.x] + kr.y] = i;
 }
 
 // recs[p] = tmp[src[p]]: the records move to their sorted positions as
 // random reads and coalesced writes (a scatter of the 16-byte records would
 // write half sectors at random addresses of an array larger than L2).
-template <typename RecT>
+template <typename RecT, bool STREAM>
 __global__ void k_bin_gather(const RecT *__restrict__ tmp, const int *__restrict__ src, int M,
                              RecT *__restrict__ recs) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= M) return;
-    recs[q] = tmp[__ldg(src + q)];
+    st_rec<STREAM>(recs + q, tmp[ld_once<STREAM>(src + q)]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1474,6 +1498,8 @@ int create_plan(nfft2d_plan_s **out, int N1, int N2, double sigma, int K, int pr
     if (cudaGetDevice(&p->device) != cudaSuccess) return fail(NFFT2D_ERR_CUDA);
     if (cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
         return fail(NFFT2D_ERR_CUDA);
+    if (cudaDeviceGetAttribute(&p->l2_bytes, cudaDevAttrL2CacheSize, p->device) != cudaSuccess)
+        return fail(NFFT2D_ERR_CUDA);
 
     // window constants (FP64, plan time)
     const double alpha = (2.0 - 1.0 / sigma) * kPi - 0.01;
@@ -1819,40 +1845,48 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     constexpr int kCellTile = kCellScanThreads * kCellScanItems, kItemTile = kItemScanThreads * kItemScanItems;
     const int scan_words = static_cast<int>(scan_state_words(p->ncells + 1, kCellTile) +
                                             scan_state_words(static_cast<size_t>(g.tiles1) * g.tiles2 + 1, kItemTile));
+    // the binning's arrays against L2: coordinates, tmp records, keys and
+    // ranks, the inverse permutation, sorted records, cell counters
+    const size_t rec_bytes = p->precision == NFFT2D_F64 ? sizeof(Rec64) : sizeof(Rec32);
+    const size_t bin_bytes = static_cast<size_t>(M) * ((coord_dtype == NFFT2D_COORD_F64 ? 16 : 8) + 2 * rec_bytes + 12) +
+                             4 * (p->ncells + 1);
+    const bool stream = bin_bytes > static_cast<size_t>(p->l2_bytes);
+    auto bin = [&](auto ct, auto rt, auto st) -> cudaError_t {
+        using CT = decltype(ct);
+        using RecT = decltype(rt);
+        constexpr bool S = decltype(st)::value;
+        k_bin_pass1<CT, RecT, S><<<blocks, 256, 0, p->stream>>>(
+            static_cast<const CT *>(x1), static_cast<const CT *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
+            static_cast<RecT *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (coords_read && (e = cudaEventRecord(coords_read, p->stream)) != cudaSuccess) return e;  // coordinates read
+        const size_t cells_n = p->ncells + 1;
+        k_scan_counts<<<static_cast<unsigned>((cells_n + kCellTile - 1) / kCellTile), kCellScanThreads, 0,
+                        p->stream>>>(p->cell_count, cells_n, scan_state, p->d_status);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        k_bin_invert<S><<<blocks, 256, 0, p->stream>>>(p->keyrank, p->cell_count, Mi, p->src);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        k_bin_gather<RecT, S><<<blocks, 256, 0, p->stream>>>(static_cast<const RecT *>(p->tmp_recs), p->src, Mi,
+                                                              static_cast<RecT *>(p->recs));
+        return cudaGetLastError();
+    };
+    using Yes = std::true_type;
+    using No = std::false_type;
+    cudaError_t be;
     if (p->precision == NFFT2D_F64) {
         if (coord_dtype == NFFT2D_COORD_F64)
-            k_bin_pass1<double, Rec64><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec64 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
+            be = stream ? bin(double{}, Rec64{}, Yes{}) : bin(double{}, Rec64{}, No{});
         else
-            k_bin_pass1<float, Rec64><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec64 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
+            be = stream ? bin(float{}, Rec64{}, Yes{}) : bin(float{}, Rec64{}, No{});
     } else {
         if (coord_dtype == NFFT2D_COORD_F64)
-            k_bin_pass1<double, Rec32><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const double *>(x1), static_cast<const double *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec32 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
+            be = stream ? bin(double{}, Rec32{}, Yes{}) : bin(double{}, Rec32{}, No{});
         else
-            k_bin_pass1<float, Rec32><<<blocks, 256, 0, p->stream>>>(
-                static_cast<const float *>(x1), static_cast<const float *>(x2), Mi, o1, o2, s1, s2, s1f, s2f, exact, g,
-                static_cast<Rec32 *>(p->tmp_recs), p->keyrank, p->cell_count, p->d_status, scan_state, scan_words);
+            be = stream ? bin(float{}, Rec32{}, Yes{}) : bin(float{}, Rec32{}, No{});
     }
-    NFFT_TRY_CUDA(cudaGetLastError());
-    if (coords_read) NFFT_TRY_CUDA(cudaEventRecord(coords_read, p->stream));  // the coordinates are read
+    NFFT_TRY_CUDA(be);
     const size_t cells_n = p->ncells + 1;
-    k_scan_counts<<<static_cast<unsigned>((cells_n + kCellTile - 1) / kCellTile), kCellScanThreads, 0, p->stream>>>(
-        p->cell_count, cells_n, scan_state, p->d_status);
-    NFFT_TRY_CUDA(cudaGetLastError());
-    k_bin_invert<<<blocks, 256, 0, p->stream>>>(p->keyrank, p->cell_count, Mi, p->src);
-    NFFT_TRY_CUDA(cudaGetLastError());
-    if (p->precision == NFFT2D_F64)
-        k_bin_gather<Rec64><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec64 *>(p->tmp_recs), p->src, Mi,
-                                                           static_cast<Rec64 *>(p->recs));
-    else
-        k_bin_gather<Rec32><<<blocks, 256, 0, p->stream>>>(static_cast<const Rec32 *>(p->tmp_recs), p->src, Mi,
-                                                           static_cast<Rec32 *>(p->recs));
-    NFFT_TRY_CUDA(cudaGetLastError());
     const int ntiles = g.tiles1 * g.tiles2;
     k_scan_emit_chunks<<<static_cast<unsigned>((ntiles + 1 + kItemTile - 1) / kItemTile), kItemScanThreads, 0,
                          p->stream>>>(p->cell_count, ntiles, g.T * g.T, p->chunk, p->chunks,

@@ -890,6 +890,13 @@ def run_ours(args, wl):
                 "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": dom_ms,
                 "traffic": ncu_traffic(kname, wl["name"])}
+    # the same kernel with the per-point arrays in the plan's binned order
+    # (io_order binned): no random 8-byte accesses to f
+    tb = ncu_traffic(kname + "_binned", wl["name"])
+    if tb is not None:
+        roofline["traffic_binned_io"] = tb
+        roofline["traffic_note"] = ("traffic: caller-order f (random 8-byte accesses, one sector each); "
+                                    "traffic_binned_io: f in the binned order (the binned_io arm)")
 
     # ---- e2e through the public API with pinned host buffers ----
     e2e = None

@@ -788,7 +788,7 @@ def run_ours(args, wl):
         # one transform of world * M points: each rank draws its own M points
         # (the workload's distribution, a rank-specific seed) and keeps them
         if wl["name"].startswith("clustered"):
-            wl = clustered_config3(seed=3 + 1000 * rank, K=wl["K"])
+            wl = clustered_config3(seed=3 + 1000 * rank, K=wl["K"], M=wl["x1"].size)
         elif wl["name"].startswith("polar"):
             wl = polar_raster(seed=2 + 1000 * rank, K=wl["K"])
     dev = torch.device("cuda", local)
@@ -1789,13 +1789,24 @@ def main():
                          "a copy (copy); auto picks the faster by an untimed trial of each")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
+    ap.add_argument("--points", type=int, default=None,
+                    help="clustered workload only: this many points instead of 2^24 (same grid and seed), "
+                         "for profiler captures of the same kernels on a smaller working set")
     ap.add_argument("--K", type=int, default=None,
                     help="window half-width for the clustered and polar workloads (2..8; default 6)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    wl = (WORKLOADS[args.workload](K=args.K) if (args.workload in ("clustered", "polar") and args.K)
-          else WORKLOADS[args.workload]())
+    if args.points is not None and args.workload != "clustered":
+        ap.error("--points applies to the clustered workload only")
+    if args.workload == "clustered":
+        kw = {} if args.K is None else {"K": args.K}
+        if args.points is not None:
+            kw["M"] = args.points
+        wl = clustered_config3(**kw)
+    else:
+        wl = (WORKLOADS[args.workload](K=args.K) if (args.workload == "polar" and args.K)
+              else WORKLOADS[args.workload]())
     if args.workload == "ffbp":
         if args.impl == "reference":
             run_ffbp_reference(args, wl)

@@ -585,6 +585,8 @@ def cpu_baseline_isolated(args, steps: int = 10):
            "--steps", str(steps), "--warmup", "3", "--no-reference-gpu"]
     if args.K:
         cmd += ["--K", str(args.K)]
+    if getattr(args, "points", None):
+        cmd += ["--points", str(args.points)]
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE")}
     env["CUDA_VISIBLE_DEVICES"] = ""
     try:

@@ -50,3 +50,9 @@ def test_library_line_cpu_baseline_is_the_reference_arm_in_a_child():
     assert "unavailable" not in cb, cb
     assert cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1 and cb["sample"]
     assert cb["extrapolated"] is False and "child process" in cb["process"]
+
+
+def test_points_option_is_for_the_clustered_workload_only():
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "polar",
+                          "--points", "1000"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 2 and "--points" in out.stderr

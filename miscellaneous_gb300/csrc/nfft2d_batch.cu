@@ -38,7 +38,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kSpreadWarps = 4;
-constexpr int kSpreadItem = 128;
 
 // One transform of a batch, device resident (the tensor map needs 64-byte
 // alignment; the struct keeps it first and the array is allocated aligned).
@@ -223,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, K <= 6 ? 4 : 3)  // as the single-pl
 template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32)
     k_batch_spread(const BatchDesc *__restrict__ d, int first, int n, const BatchIO *__restrict__ io, int chunk0,
-                   int total, Geom g0, const __grid_constant__ WinPoly wp, int chunk, int *work, int *status) {
+                   int total, Geom g0, const __grid_constant__ WinPoly wp, int *work, int *status) {
     extern __shared__ unsigned char smem_raw[];
     using S = SpreadGeo<K>;
     unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
@@ -232,23 +231,17 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     float2 *bufs = reinterpret_cast<float2 *>(base) + warp * S::NBUF * S::PATCH;
     float *scr = reinterpret_cast<float *>(reinterpret_cast<float2 *>(base) + kSpreadWarps * S::NBUF * S::PATCH) +
                  warp * S::ROWS * S::SP;
-    const int parts = (chunk + kSpreadItem - 1) / kSpreadItem;
     StripFlush fs{nullptr, bufs, g0.H, 0};
     strip_flush_init<K>(fs, scr);
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(work, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= total * parts) break;
-        const int gl = item / parts, part = item - gl * parts;
+    for (;;) {  // a warp's work item is one whole chunk, as in the single-plan spread
+        int gl = 0;
+        if (lane == 0) gl = atomicAdd(work, 1);
+        gl = __shfl_sync(0xffffffffu, gl, 0);
+        if (gl >= total) break;
         const int gc = chunk0 + gl;
         const int t = first + find_transform<0>(d + first, n, gc);
         const BatchDesc &D = d[t];
-        int4 ch = __ldg(&D.chunks[gc - D.chunk_base]);
-        const int first = part * kSpreadItem;
-        if (first >= ch.z) continue;
-        ch.y += first;
-        ch.z = min(kSpreadItem, ch.z - first);
+        const int4 ch = __ldg(&D.chunks[gc - D.chunk_base]);
         const int tr = ch.x / D.g.tiles2, tc = ch.x - tr * D.g.tiles2;
         fs.map = &D.tmap;  // this transform's grid (strip-patch box)
         spread_item<K>(D.recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, io[t].in, 0, scr, fs, wp, status);
@@ -371,13 +364,12 @@ int launch_spread(nfft2d_batch_s *b, const nfft2d_batch_s::KGroup &kg, int sms) 
     if (smem > 48 * 1024) B_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
     B_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSpreadWarps * 32, smem));
-    const int chunk = b->plans[kg.first]->chunk;
-    const long long items = static_cast<long long>(kg.total_chunks) * ((chunk + kSpreadItem - 1) / kSpreadItem);
+    const long long items = kg.total_chunks;
     const int blocks = static_cast<int>(std::max(1LL, std::min<long long>((items + kSpreadWarps - 1) / kSpreadWarps,
                                                                     std::max(per_sm, 1) * sms)));
     B_TRY(cudaMemsetAsync(b->d_work, 0, sizeof(int), b->stream));
     kernel<<<blocks, kSpreadWarps * 32, smem, b->stream>>>(b->d_desc, kg.first, kg.n, b->d_io, kg.chunk0,
-                                                           kg.total_chunks, kg.g0, kg.poly, chunk, b->d_work,
+                                                           kg.total_chunks, kg.g0, kg.poly, b->d_work,
                                                            b->d_status);
     B_TRY(cudaGetLastError());
     return NFFT2D_OK;

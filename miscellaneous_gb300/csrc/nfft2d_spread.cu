@@ -41,7 +41,6 @@ namespace {
 constexpr int kThreads = 256;
 
 constexpr int kSpreadWarps = 4;  // warps per CTA of the tiled spread
-constexpr int kSpreadItem = 128; // points per warp work item (a chunk is split into items)
 
 template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid_constant__ CUtensorMap tmap,
@@ -64,18 +63,17 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
     StripFlush fs{&tmap, bufs, g.H, 0};
     strip_flush_init<K>(fs, scr);
 
-    const int parts = (a.chunk + kSpreadItem - 1) / kSpreadItem;  // items per chunk
+    // A warp's work item is one whole chunk (up to the plan's chunk points
+    // of one tile): splitting chunks into fixed-size items left items
+    // empty wherever a chunk held fewer points, and split one tile's strips
+    // between warps (each flushing them) -- 1.08 against 0.97 ms at 2^24
+    // clustered points and 256-point chunks.
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(work, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= n * parts) break;
-        const int c = item / parts, part = item - c * parts;
-        int4 ch = __ldg(&chunks[c]);
-        const int first = part * kSpreadItem;
-        if (first >= ch.z) continue;  // this chunk has fewer points
-        ch.y += first;
-        ch.z = min(kSpreadItem, ch.z - first);
+        int c = 0;
+        if (lane == 0) c = atomicAdd(work, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= n) break;
+        const int4 ch = __ldg(&chunks[c]);
         const int tr = ch.x / g.tiles2, tc = ch.x - tr * g.tiles2;
         spread_item<K>(recs, ch.y, ch.z, tr * kRegTile, tc * kRegTile, f, a.binned_io, scr, fs, a.poly, a.status);
     }
@@ -135,8 +133,7 @@ cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kSpreadWarps * 32, smem);
         if (p->n_chunks >= 0) {  // else the count is on the device: the full persistent grid
-            const long long items = p->n_chunks * ((p->chunk + kSpreadItem - 1) / kSpreadItem);
-            const int need = static_cast<int>((items + kSpreadWarps - 1) / kSpreadWarps);
+            const int need = static_cast<int>((p->n_chunks + kSpreadWarps - 1) / kSpreadWarps);
             if (blocks > need) blocks = need;
         }
         kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(p->tmap_spread, static_cast<const Rec32 *>(p->recs),

@@ -810,9 +810,10 @@ def run_ours(args, wl):
         plan.set_tuning(fft_mode={"cufft": 0, "pruned": 1, "fused": 2}[args.fft_mode])
     plan.set_points(x1, x2, units="unit")
     tuned = None
-    if args.no_autotune and args.gather_variant != "auto":
+    if args.no_autotune and (args.gather_variant != "auto" or args.chunk):
         from miscellaneous_gb300 import _lib as _l
-        plan.set_tuning(gather_variant=_l.VARIANT_TILED if args.gather_variant == "tiled" else _l.VARIANT_DIRECT)
+        gv = {"auto": -1, "tiled": _l.VARIANT_TILED, "direct": _l.VARIANT_DIRECT}[args.gather_variant]
+        plan.set_tuning(gather_variant=gv, chunk=args.chunk or -1)
         plan.set_points(x1, x2, units="unit")
     if not args.no_autotune:
         from miscellaneous_gb300 import autotune
@@ -1791,6 +1792,8 @@ def main():
                          "a copy (copy); auto picks the faster by an untimed trial of each")
     ap.add_argument("--gather-variant", choices=["auto", "tiled", "direct"], default="auto",
                     help="with --no-autotune: the gather kernel to use (default: the plan's default)")
+    ap.add_argument("--chunk", type=int, default=None,
+                    help="with --no-autotune: points per work item (default: the plan's default, 256)")
     ap.add_argument("--points", type=int, default=None,
                     help="clustered workload only: this many points instead of 2^24 (same grid and seed), "
                          "for profiler captures of the same kernels on a smaller working set")

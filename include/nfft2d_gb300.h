@@ -102,7 +102,10 @@ typedef struct {
 
 typedef struct {
     int tile;              /* 0 or -1 = keep; else 8, 16, 32 or 64              */
-    int chunk;             /* 0 or -1 = keep; else points per work item (>= 32) */
+    int chunk;             /* 0 or -1 = keep; else points per work item (>= 32):
+                              a tile's points are cut into items of this many;
+                              the tiled gather stages one patch per item and
+                              the tiled spread gives each item to one warp     */
     int gather_variant;    /* -1 = keep; NFFT2D_VARIANT_* (AUTO: chosen at
                               set_points from the bin density)                  */
     int spread_variant;    /* -1 = keep; NFFT2D_VARIANT_*                       */

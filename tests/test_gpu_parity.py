@@ -105,6 +105,20 @@ def test_tile_sizes_agree(orc, tile):
     assert orc.rel_l2(adj, orc.nfft2_2d(f, g1, g2, 64, 64, sign=+1)) < 2e-6
 
 
+@pytest.mark.parametrize("chunk", [32, 100, 512, 4096])
+def test_work_item_sizes_agree(orc, chunk):
+    """The chunk is the tiled gather's patch item and the tiled spread's warp
+    item: a tile's points cut at any size give the same transforms, from items
+    of a few points to one item per dense tile."""
+    F, x1, x2, f = _inputs(64, 64, 6000, seed=12, dist="cluster")
+    fwd, adj, _, info = _run({"sigma": 2.0, "K": 6}, F, x1, x2, f,
+                             tuning={"chunk": chunk, "gather_variant": 1, "spread_variant": 1})
+    assert info["chunk"] == chunk and info["gather_variant"] == 1 and info["spread_variant"] == 1
+    g1, g2 = _grid(x1, 64), _grid(x2, 64)
+    assert orc.rel_l2(fwd, orc.nfft1_2d(F, g1, g2, sign=-1)) < 2e-6
+    assert orc.rel_l2(adj, orc.nfft2_2d(f, g1, g2, 64, 64, sign=+1)) < 2e-6
+
+
 def test_direct_variant_matches_tiled(orc):
     F, x1, x2, f = _inputs(64, 32, 2000, seed=4)
     t = _run({"sigma": 2.0, "K": 6}, F, x1, x2, f)

@@ -9,7 +9,9 @@ same shape reuse them without measuring.
 
 Candidates: the gather variant (TMA-tiled shared-memory patches, or direct
 L1/L2 reads of the padded grid) and the work-item size (points per tile work
-item).  The tile edge stays at 16, which the register-resident spread needs.
+item; above 512 points the spread keeps items of 512, the tiled gather takes
+the larger ones).  The tile edge stays at 16, which the register-resident
+spread needs.
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ _DEFAULT_CANDIDATES = (
     dict(gather_variant=_lib.VARIANT_TILED, chunk=256),
     dict(gather_variant=_lib.VARIANT_TILED, chunk=128),
     dict(gather_variant=_lib.VARIANT_TILED, chunk=512),
+    dict(gather_variant=_lib.VARIANT_TILED, chunk=2048),  # the spread then cuts its own 512-point items
     dict(gather_variant=_lib.VARIANT_DIRECT, chunk=256),
     dict(gather_variant=_lib.VARIANT_DIRECT, chunk=128),
 )

@@ -70,6 +70,9 @@ __host__ __device__ constexpr int pow2_floor(int v) {
     return p;
 }
 __host__ __device__ constexpr int spread_strip_width(int K) { return pow2_floor(spread_group_lanes(K) - 2 * K); }
+// Largest work item of the tiled spread: plans with larger chunks (which the
+// tiled gather prefers) get a second work list cut at this size.
+constexpr int kSpreadItemMax = 512;
 
 // Geometry shared by kernels.
 struct Geom {
@@ -135,6 +138,10 @@ struct nfft2d_plan_s {
     int *src = nullptr;          // per sorted position: the caller index
     int4 *chunks = nullptr;
     long long chunks_cap = 0;
+    // the tiled spread's work items when chunk > kSpreadItemMax: the same
+    // tiles cut into items of kSpreadItemMax points (count in d_status[3])
+    int4 *items = nullptr;
+    long long items_cap = 0;
     long long n_chunks = 0;
     double xscale1 = 1.0, xscale2 = 1.0;  // dt/dx for the units given to set_points
 

@@ -969,11 +969,12 @@ __global__ void __launch_bounds__(kCellScanThreads) k_scan_counts(unsigned *__re
 // Work items from the scanned cell starts: tile t (cells_per_tile cells from
 // t * cells_per_tile) holds ceil(count / chunk) items of up to `chunk`
 // points.  One scan over the per-tile item counts places every tile's items;
-// the thread owning index ntiles stores the total in status[0].
+// the thread owning index ntiles stores the total in *total.
 __global__ void __launch_bounds__(kItemScanThreads, 1) k_scan_emit_chunks(const unsigned *__restrict__ cell_start,
                                                                        int ntiles, int cells_per_tile, int chunk,
                                                                        int4 *__restrict__ chunks,
-                                                                       unsigned long long *state, int *status) {
+                                                                       unsigned long long *state, int *status,
+                                                                       int *total) {
     static_assert(kItemScanItems == 1, "one bin tile per thread");
     const int tile = scan_ticket(state);
     const long long t = static_cast<long long>(tile) * kItemScanThreads + threadIdx.x;  // bin tile
@@ -985,7 +986,7 @@ __global__ void __launch_bounds__(kItemScanThreads, 1) k_scan_emit_chunks(const 
         v[0] = (cnt + chunk - 1) / chunk;
     }
     const unsigned run = block_scan_lookback<kItemScanThreads, 1>(v, tile, state, status);
-    if (t == ntiles) status[0] = static_cast<int>(run);
+    if (t == ntiles) *total = static_cast<int>(run);
     for (unsigned c = 0; c < v[0]; ++c) {
         const unsigned off = c * chunk;
         chunks[run + c] = make_int4(static_cast<int>(t), static_cast<int>(start + off),
@@ -997,13 +998,16 @@ __global__ void __launch_bounds__(kItemScanThreads, 1) k_scan_emit_chunks(const 
 // plan helpers
 // ---------------------------------------------------------------------------
 void free_points(nfft2d_plan_s *p) {
-    if (p->recs || p->tmp_recs || p->keyrank || p->src || p->chunks)
+    if (p->recs || p->tmp_recs || p->keyrank || p->src || p->chunks || p->items)
         cudaStreamSynchronize(p->stream);  // no transform of the old points in flight
     plan_free(p->recs);
     plan_free(p->tmp_recs);
     plan_free(p->keyrank);
     plan_free(p->src);
     plan_free(p->chunks);
+    plan_free(p->items);
+    p->items = nullptr;
+    p->items_cap = 0;
     p->recs = p->tmp_recs = nullptr;
     p->keyrank = nullptr;
     p->src = nullptr;
@@ -1056,9 +1060,16 @@ long long chunks_capacity(const nfft2d_plan_s *p, long long M) {
     return static_cast<long long>(p->g.tiles1) * p->g.tiles2 + M / p->chunk + 1;
 }
 
+// Capacity of the spread's own work list (plans whose chunk exceeds
+// kSpreadItemMax), 0 when the chunks serve the spread.
+long long items_capacity(const nfft2d_plan_s *p, long long M) {
+    if (p->chunk <= kSpreadItemMax) return 0;
+    return static_cast<long long>(p->g.tiles1) * p->g.tiles2 + M / kSpreadItemMax + 1;
+}
+
 int ensure_points_capacity(nfft2d_plan_s *p, long long M) {
     const long long need_chunks = chunks_capacity(p, M);
-    if (M <= p->capM && need_chunks <= p->chunks_cap) return NFFT2D_OK;
+    if (M <= p->capM && need_chunks <= p->chunks_cap && items_capacity(p, M) <= p->items_cap) return NFFT2D_OK;
     free_points(p);
     const long long cap = std::max<long long>(M, 1);
     const size_t rs = rec_size(p->precision);
@@ -1068,15 +1079,18 @@ int ensure_points_capacity(nfft2d_plan_s *p, long long M) {
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->src), sizeof(int) * cap));
     const long long cc = chunks_capacity(p, cap);
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->chunks), sizeof(int4) * cc));
+    const long long ic = items_capacity(p, cap);
+    if (ic > 0) NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->items), sizeof(int4) * ic));
     p->capM = cap;
     p->chunks_cap = cc;
+    p->items_cap = ic;
     return NFFT2D_OK;
 }
 
 size_t plan_workspace_bytes(const nfft2d_plan_s *p) {
     const size_t grid = cplx_size(p->precision) * static_cast<size_t>(p->g.Ra) * p->g.C;
     const size_t pts = static_cast<size_t>(p->capM) * (2 * rec_size(p->precision) + sizeof(uint2) + sizeof(int)) +
-                       static_cast<size_t>(p->chunks_cap) * sizeof(int4);
+                       static_cast<size_t>(p->chunks_cap + p->items_cap) * sizeof(int4);
     const size_t bins = sizeof(unsigned) * (p->ncells + 1 + p->scan_tmp_elems);
     return grid + pts + bins + real_size(p->precision) * (p->N1 + p->N2);
 }
@@ -1157,8 +1171,9 @@ int setup_bins(nfft2d_plan_s *p) {
     p->ncells = static_cast<size_t>(g.tiles1) * g.tiles2 * g.T * g.T;
     const size_t ntiles = static_cast<size_t>(g.tiles1) * g.tiles2;
     // two 64-bit scan states (cells, work items), counted in 32-bit words
+    // 64-bit state words of three scans: cells, work items, the spread's own items
     p->scan_tmp_elems = 2 * (scan_state_words(p->ncells + 1, kCellScanThreads * kCellScanItems) +
-                             scan_state_words(ntiles + 1, kItemScanThreads * kItemScanItems));
+                             2 * scan_state_words(ntiles + 1, kItemScanThreads * kItemScanItems));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->cell_count), sizeof(unsigned) * (p->ncells + 1)));
     NFFT_TRY_CUDA(plan_malloc(reinterpret_cast<void **>(&p->scan_tmp), sizeof(unsigned) * p->scan_tmp_elems));
     return NFFT2D_OK;
@@ -1843,8 +1858,8 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     // ticket + tile words of the cell scan, then of the work-item scan
     unsigned long long *scan_state = reinterpret_cast<unsigned long long *>(p->scan_tmp);
     constexpr int kCellTile = kCellScanThreads * kCellScanItems, kItemTile = kItemScanThreads * kItemScanItems;
-    const int scan_words = static_cast<int>(scan_state_words(p->ncells + 1, kCellTile) +
-                                            scan_state_words(static_cast<size_t>(g.tiles1) * g.tiles2 + 1, kItemTile));
+    const size_t item_words = scan_state_words(static_cast<size_t>(g.tiles1) * g.tiles2 + 1, kItemTile);
+    const int scan_words = static_cast<int>(scan_state_words(p->ncells + 1, kCellTile) + 2 * item_words);
     // the binning's arrays against L2: coordinates, tmp records, keys and
     // ranks, the inverse permutation, sorted records, cell counters
     const size_t rec_bytes = p->precision == NFFT2D_F64 ? sizeof(Rec64) : sizeof(Rec32);
@@ -1888,10 +1903,17 @@ int nfft2d::set_points_scaled(nfft2d_plan_s *p, long long M, const void *x1, con
     NFFT_TRY_CUDA(be);
     const size_t cells_n = p->ncells + 1;
     const int ntiles = g.tiles1 * g.tiles2;
-    k_scan_emit_chunks<<<static_cast<unsigned>((ntiles + 1 + kItemTile - 1) / kItemTile), kItemScanThreads, 0,
-                         p->stream>>>(p->cell_count, ntiles, g.T * g.T, p->chunk, p->chunks,
-                                      scan_state + scan_state_words(cells_n, kCellTile), p->d_status);
+    const unsigned emit_blocks = static_cast<unsigned>((ntiles + 1 + kItemTile - 1) / kItemTile);
+    unsigned long long *item_state = scan_state + scan_state_words(cells_n, kCellTile);
+    k_scan_emit_chunks<<<emit_blocks, kItemScanThreads, 0, p->stream>>>(
+        p->cell_count, ntiles, g.T * g.T, p->chunk, p->chunks, item_state, p->d_status, p->d_status);
     NFFT_TRY_CUDA(cudaGetLastError());
+    if (p->chunk > kSpreadItemMax) {  // the spread's own work list, count in status[3]
+        k_scan_emit_chunks<<<emit_blocks, kItemScanThreads, 0, p->stream>>>(
+            p->cell_count, ntiles, g.T * g.T, kSpreadItemMax, p->items, item_state + item_words, p->d_status,
+            p->d_status + 3);
+        NFFT_TRY_CUDA(cudaGetLastError());
+    }
     stage_end(p, ST_SORT);
     if (p->gather_auto) p->gather_variant = auto_gather(p, M);
     if (async) {

@@ -45,7 +45,8 @@ constexpr int kSpreadWarps = 4;  // warps per CTA of the tiled spread
 template <int K>
 __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid_constant__ CUtensorMap tmap,
                                                                     const Rec32 *__restrict__ recs,
-                                                                    const int4 *__restrict__ chunks,
+                                                                    const int4 *__restrict__ chunks, int n_host,
+                                                                    const int *__restrict__ n_dev,
                                                                     const float2 *__restrict__ f,
                                                                     const __grid_constant__ KArgs a) {
     extern __shared__ unsigned char smem_raw[];
@@ -58,16 +59,18 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_tiled(const __grid
     float2 *bufs = reinterpret_cast<float2 *>(base) + warp * S::NBUF * S::PATCH;
     float *scr = reinterpret_cast<float *>(reinterpret_cast<float2 *>(base) + kSpreadWarps * S::NBUF * S::PATCH) +
                  warp * S::ROWS * S::SP;
-    const int n = a.n_chunks >= 0 ? a.n_chunks : a.status[0];  // < 0: counted on the device only
+    const int n = n_host >= 0 ? n_host : *n_dev;  // < 0: counted on the device only
     int *work = a.status + 2;  // work-item counter, zeroed before the launch
     StripFlush fs{&tmap, bufs, g.H, 0};
     strip_flush_init<K>(fs, scr);
 
-    // A warp's work item is one whole chunk (up to the plan's chunk points
-    // of one tile): splitting chunks into fixed-size items left items
-    // empty wherever a chunk held fewer points, and split one tile's strips
-    // between warps (each flushing them) -- 1.08 against 0.97 ms at 2^24
-    // clustered points and 256-point chunks.
+    // A warp's work item is one whole entry of the work list: the plan's
+    // chunks (up to `chunk` points of one tile), or for chunks above
+    // kSpreadItemMax the binning's second list cut at that size.  Splitting
+    // chunks into fixed-size parts instead left parts empty wherever a chunk
+    // held fewer points, and split one tile's strips between warps (each
+    // flushing them) -- 1.08 against 0.97 ms at 2^24 clustered points and
+    // 256-point chunks.
     for (;;) {
         int c = 0;
         if (lane == 0) c = atomicAdd(work, 1);
@@ -132,12 +135,15 @@ cudaError_t launch_K(const nfft2d_plan_s *p, const void *f) {
         cudaError_t e = cudaMemsetAsync(p->d_status + 2, 0, sizeof(int), p->stream);
         if (e != cudaSuccess) return e;
         int blocks = grid_blocks(p, reinterpret_cast<const void *>(kernel), kSpreadWarps * 32, smem);
-        if (p->n_chunks >= 0) {  // else the count is on the device: the full persistent grid
-            const int need = static_cast<int>((p->n_chunks + kSpreadWarps - 1) / kSpreadWarps);
+        const bool own_list = p->chunk > kSpreadItemMax;  // its count stays on the device (status[3])
+        const int n_host = own_list ? -1 : static_cast<int>(p->n_chunks);
+        if (n_host >= 0) {  // else the count is on the device: the full persistent grid
+            const int need = (n_host + kSpreadWarps - 1) / kSpreadWarps;
             if (blocks > need) blocks = need;
         }
-        kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(p->tmap_spread, static_cast<const Rec32 *>(p->recs),
-                                                                p->chunks, static_cast<const float2 *>(f), a);
+        kernel<<<blocks, kSpreadWarps * 32, smem, p->stream>>>(
+            p->tmap_spread, static_cast<const Rec32 *>(p->recs), own_list ? p->items : p->chunks, n_host,
+            p->d_status + (own_list ? 3 : 0), static_cast<const float2 *>(f), a);
         return cudaGetLastError();
     }
     const int blocks = static_cast<int>((p->M + kThreads - 1) / kThreads);

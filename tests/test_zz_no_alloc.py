@@ -15,6 +15,7 @@ free memory and torch's allocation count unchanged.  This file is collected
 last on purpose.
 """
 import ctypes
+import gc
 
 import numpy as np
 import pytest
@@ -114,8 +115,16 @@ def test_noalloc_call_allocates_no_device_memory(lib):
         torch.cuda.synchronize()
 
     call()
-    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
-    for _ in range(3):
-        call()
-    assert torch.cuda.mem_get_info()[0] == free0
-    assert torch.cuda.memory_allocated() == alloc0
+    # tensors of earlier tests that the cyclic collector frees in the middle
+    # would change torch's count without any allocation by the call
+    gc.collect()
+    gc.disable()
+    try:
+        free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+        for _ in range(3):
+            call()
+        free1, alloc1 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    finally:
+        gc.enable()
+    assert free1 == free0
+    assert alloc1 == alloc0

@@ -1009,6 +1009,7 @@ def run_ours(args, wl):
         cu = statistics.median(cu_ms)
         e2e = {"value": world * M / (te * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te,
+               "ms_per_step_min_median_max": [min(e_ms), statistics.median(e_ms), max(e_ms)],
                "coords_upload_ms": cu, "coords_upload_gbs": (hx1.numel() + hx2.numel()) * 4 / (cu * 1e-3) / 1e9,
                "coords": "direct" if mode["direct"] else "copy", "coords_trial_ms": trial,
                "includes": "H2D of the coordinates (read by the binning pass over the link with coords "
